@@ -1,0 +1,301 @@
+"""Benchmark of the path-tracing pass: Mrays/s on the instanced 1920x1080 workload.
+
+Workload (default, one GPU): 16 seeded meshes (~4.9M unique triangles, noise-displaced
+icospheres and heightfield grids) in 1024 instances (~68M instanced triangles), a 2048x1024
+RGBA32F procedural sky with a 0.5 degree sun disc, 1920x1080 pinhole camera, 64 samples
+per pixel, 8 bounces, the reference's Russian roulette (contribution factor 4).  A step is
+one full frame: invalidate + 64 dispatches' worth of samples, so every step renders the
+same 132.7M paths.  Mrays/s counts traversal queries (primary + extension rays).
+
+  value  device-resident: scene, environment and image stay in HBM; CUDA events bracket K
+         steps on the launching stream.  The scene (~0.8 GB) and the path queues exceed L2,
+         so no flush is needed between steps.
+  e2e    the same frames through the C ABI with host buffers: the camera struct goes in and
+         the 33 MB RGBA32F image comes back to pinned host memory inside every step.
+
+--impl reference times the CPU restatement of the reference pass (oracle/, all host
+threads) on crops of the same frame.  --gpus N runs N independent replicas (one frame each,
+weak scaling); there is no data-path collective.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = "Mrays/s (primary + extension rays), 1920x1080 64spp 8 bounces"
+UNIT = "Mrays/s"
+WORKLOAD = "instanced 16 meshes / 1024 instances, 1920x1080, 64 spp, 8 bounces, equirect sky"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU work per baseline sample")
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--spp", type=int, default=64)
+    return p.parse_args()
+
+
+def dist_env():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while the timed region runs."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+              "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+              "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.FIELDS}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 7:
+                self.rows.append(parts)
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"], "samples": 0}
+        sm = [float(r[0]) for r in self.rows if r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4) if r[3 + k].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.rows)}
+
+
+def measured_peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            p = json.load(f)
+        return float(p["hbm_gbs"]), "measured"
+    except (OSError, KeyError, ValueError):
+        return 6800.0, "fallback"
+
+
+def build_workload(spp):
+    from nbounce_gb300 import scenes
+    desc = scenes.instanced_scene(spp=spp)
+    return desc
+
+
+def cpu_baseline(desc, sobol, seconds, threads):
+    """The oracle (binary32 restatement of the reference pass) on a centred crop of the frame,
+    sized from a calibration run to take about `seconds`.  Returns a dict for the JSON line
+    plus the reference work counters per ray."""
+    from oracle import oracle as O
+    t0 = time.perf_counter()
+    osc = O.OracleScene(desc.vertices, desc.indices, desc.primitives(), dedup=True)
+    build_s = time.perf_counter() - t0
+    W, H, spp = desc.width, desc.height, desc.spp
+
+    def run(w, h):
+        x0, y0 = (W - w) // 2, (H - h) // 2
+        t = time.perf_counter()
+        _, rays, _, _ = osc.render(desc.clip_to_world, W, H, sobol, 1, spp, bounces=desc.bounces,
+                                   env_texels=desc.env_texels, region=(x0, y0, w, h), threads=threads)
+        return rays, time.perf_counter() - t
+
+    rays, dt = run(16, 16)
+    scale = max(1.0, seconds / max(dt, 1e-3))
+    side = int(16 * scale ** 0.5) // 8 * 8
+    w, h = min(W, max(16, side * 2)), min(H, max(16, side // 2))
+    rays, dt = run(w, h)
+    per_ray = osc.work_per_ray()
+    return {"value": rays / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"centred {w}x{h} crop of the 1920x1080 frame, {spp} spp, {rays} rays in {dt:.1f} s "
+                      f"(oracle scene build {build_s:.1f} s, not timed)"}, per_ray, osc
+
+
+def run_ours(args):
+    import torch
+    import nbounce_gb300 as nb
+
+    rank, world, local = dist_env()
+    if world > 1:
+        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    desc = build_workload(args.spp)
+    t0 = time.perf_counter()
+    scene = nb.SceneBuffers.from_desc(desc, dedup=True)
+    build_s = time.perf_counter() - t0
+    env = nb.EnvMap(texels=desc.env_texels)
+    cam = nb.camera_struct(desc.world_to_clip, desc.clip_to_world)
+    pt = nb.Pathtracer(desc.width, desc.height, nb.Globals(bounces=desc.bounces))
+    stream = torch.cuda.current_stream(dev)
+    sh = stream.cuda_stream
+
+    def step():
+        pt.invalidate()
+        pt.render(scene, cam, env, desc.spp, stream=sh)
+
+    for _ in range(max(3, args.warmup)):
+        step()
+    rays_per_step, status = pt.last_stats(stream=sh)
+    if status:
+        raise RuntimeError(f"device status {status}")
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    # device-resident timing, per-kernel events on the launch stream
+    pt.enable_timing(True)
+    pt.kernel_times(reset=True, stream=sh)
+    torch.cuda.synchronize()
+    barrier()
+    start, stop = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clocks:
+        start.record(stream)
+        for _ in range(args.steps):
+            step()
+        stop.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    ms = start.elapsed_time(stop)
+    kt = pt.kernel_times(reset=True, stream=sh)
+    pt.enable_timing(False)
+
+    # end-to-end through the C ABI with host buffers
+    host_img = torch.empty((desc.height, desc.width, 4), dtype=torch.float32, pin_memory=True)
+    host_np = host_img.numpy()
+    torch.cuda.synchronize()
+    barrier()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+        pt.download(out=host_np, stream=sh)
+    e2e_s = time.perf_counter() - t
+    barrier()
+
+    t_max = ms
+    e2e_max = e2e_s
+    if world > 1:
+        v = torch.tensor([ms, e2e_s], device=dev, dtype=torch.float64)
+        torch.distributed.all_reduce(v, op=torch.distributed.ReduceOp.MAX)
+        t_max, e2e_max = float(v[0]), float(v[1])
+    total_rays = rays_per_step * args.steps * world
+    value = total_rays / (t_max / 1e3) / 1e6
+    e2e_value = total_rays / e2e_max / 1e6
+    if rank != 0:
+        return None
+    launches_per_step = sum(kt[k] for k in ("raygen_launches", "trace_launches", "shade_launches",
+                                             "accumulate_launches")) / args.steps
+    line = {
+        "metric": METRIC, "value": round(value, 2), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(3, args.warmup), "ms_per_step": round(t_max / args.steps, 3), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+        "config": {"workload": WORKLOAD, "width": desc.width, "height": desc.height, "spp": desc.spp,
+                   "bounces": desc.bounces, "unique_triangles": int(desc.n_triangles_unique),
+                   "instanced_triangles": int(desc.n_triangles_instanced), "instances": len(desc.instances),
+                   "rays_per_step": int(rays_per_step), "parallelism": f"replicas x{world}",
+                   "l2": "inputs larger than L2 (scene ~0.8 GB + path queues), no flush",
+                   "scene_build_s": round(build_s, 2)},
+        "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": 128,
+                "d2h_bytes_per_step": int(desc.width * desc.height * 16)},
+        "gpu_launches": int(round(launches_per_step * args.steps)),
+        "kernel_ms_per_step": {k: round(kt[k] / args.steps, 3) for k in ("raygen_ms", "trace_ms", "shade_ms",
+                                                                       "accumulate_ms")},
+        "clocks": clocks.summary(),
+    }
+    peak, peak_kind = measured_peaks()
+    sobol = nb.sobol_burley_table()
+    if not args.no_cpu_baseline:
+        base, per_ray, _ = cpu_baseline(desc, sobol, args.cpu_seconds, os.cpu_count() or 1)
+        line["cpu_baseline"] = base
+        n_aabb, n_tri, n_inst = per_ray
+        bytes_per_ray = 32.0 * n_aabb + 48.0 * n_tri + 128.0 * n_inst  # reference-layout bytes per query
+        trace_launches = max(1, kt["trace_launches"])
+        avg_launch_ms = kt["trace_ms"] / trace_launches
+        rays_per_launch = rays_per_step * args.steps / trace_launches
+        achieved = bytes_per_ray * rays_per_launch / (avg_launch_ms / 1e3) / 1e9
+        line["roofline"] = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                            "frac": round(achieved / peak, 4), "traffic": None,
+                            "kernel": "k_trace_wave", "peak_kind": f"{peak_kind} hbm_gbs (burst copy)",
+                            "bytes_per_ray": round(bytes_per_ray, 1),
+                            "work_per_ray": {"n_aabb": round(n_aabb, 2), "n_tri": round(n_tri, 2),
+                                             "n_inst": round(n_inst, 2)}}
+    return line
+
+
+def run_reference(args):
+    rank, world, _ = dist_env()
+    if rank != 0:
+        return None
+    import nbounce_gb300 as nb
+    desc = build_workload(args.spp)
+    sobol = nb.sobol_burley_table()
+    threads = os.cpu_count() or 1
+    base, per_ray, osc = cpu_baseline(desc, sobol, min(args.cpu_seconds, 10.0), threads)
+    # time steps: each step one crop sample of the same frame
+    W, H = desc.width, desc.height
+    w, h = 64, 32
+    x0, y0 = (W - w) // 2, (H - h) // 2
+    for _ in range(args.warmup):
+        osc.render(desc.clip_to_world, W, H, sobol, 1, desc.spp, bounces=desc.bounces, env_texels=desc.env_texels,
+                   region=(x0, y0, w, h), threads=threads)
+    total_rays, t = 0, time.perf_counter()
+    for _ in range(args.steps):
+        _, rays, _, _ = osc.render(desc.clip_to_world, W, H, sobol, 1, desc.spp, bounces=desc.bounces,
+                                   env_texels=desc.env_texels, region=(x0, y0, w, h), threads=threads)
+        total_rays += rays
+    dt = time.perf_counter() - t
+    value = total_rays / dt / 1e6
+    return {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(dt / args.steps * 1e3, 2), "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded scene generator)",
+            "impl": "reference",
+            "config": {"workload": WORKLOAD, "width": W, "height": H, "spp": desc.spp, "bounces": desc.bounces,
+                       "step_sample": f"centred {w}x{h} crop per step"},
+            "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": f"centred {w}x{h} crop of the frame per step, {desc.spp} spp"},
+            "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    args = parse()
+    line = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if line is not None:
+        print(json.dumps(line), flush=True)
+
+
+if __name__ == "__main__":
+    main()

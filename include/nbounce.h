@@ -1,0 +1,262 @@
+/*
+ * nbounce.h - C ABI of the GB300-native nBounce path-tracing pass.
+ *
+ * This library is a drop-in for the reference's path-tracing compute pass
+ * (julcst/nbounce, src/pathtracing/pathtracer.rs + pathtracing.wgsl + raytracing_sw.wgsl +
+ * common.wgsl, with the scene/BVH assembly of src/pathtracing/scene.rs and bvh.rs).
+ * A Rust caller binds these symbols with an `extern "C"` block.
+ *
+ * Conventions
+ *  - Every entry point returns an nb_status; NB_OK is 0.  On error, nb_last_error() returns a
+ *    thread-local message.  Nothing aborts or traps.
+ *  - Matrices are 16 floats, column-major (glam's Mat4 memory layout).
+ *  - `stream` arguments are cudaStream_t passed as void*; NULL means the legacy default stream.
+ *    Work is stream-ordered; entry points that return host data synchronise that stream.
+ *  - Host arrays passed to *_create calls are only read during the call.  The library owns all
+ *    device memory it allocates; handles are freed with the matching *_destroy.
+ */
+#ifndef NBOUNCE_H
+#define NBOUNCE_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NB_VERSION 100
+
+/* Status codes (the reference returns Result<(), MeshError> from scene.rs:69-98 and panics
+ * elsewhere; this ABI turns every failure into a code). */
+typedef enum nb_status {
+  NB_OK = 0,
+  NB_ERR_INVALID_ARG = 1,     /* bad pointer, size, index or layout */
+  NB_ERR_OOM = 2,             /* device or host allocation failed */
+  NB_ERR_CUDA = 3,            /* a CUDA runtime call failed */
+  NB_ERR_TIMEOUT = 4,         /* a bounded device loop gave up (traversal iteration cap) */
+  NB_ERR_STACK_OVERFLOW = 5,  /* a traversal stack overflowed; results of that launch are suspect */
+  NB_ERR_NO_DEVICE = 6,       /* no CUDA device is available */
+  NB_ERR_EXHAUSTED = 7        /* the Sobol table has no rows left (sample >= max_sample_count) */
+} nb_status;
+
+/* ---------------------------------------------------------------------------------------
+ * Reference data layouts (byte-compatible with the reference's bytemuck uploads)
+ * ------------------------------------------------------------------------------------- */
+
+/* src/pathtracing/scene.rs:13-21 (48 bytes) */
+typedef struct nb_vertex {
+  float position[3];
+  float u;
+  float normal[3];
+  float v;
+  float tangent[4];
+} nb_vertex;
+
+/* src/pathtracing/bvh.rs:15-24 (32 bytes).  Leaf iff end > 0, covering primitives
+ * [start, end); an inner node has end == 0 and children start, start + 1. */
+typedef struct nb_bvh_node {
+  float min[3];
+  uint32_t start;
+  float max[3];
+  uint32_t end;
+} nb_bvh_node;
+
+/* src/pathtracing/scene.rs:220-230 (160 bytes), stored in TLAS-permuted order. */
+typedef struct nb_instance {
+  float world_to_local[16];
+  float local_to_world[16];
+  float color[4];
+  float roughness;
+  float metallic;
+  float emissive;
+  uint32_t node; /* BLAS root node index */
+} nb_instance;
+
+/* One glTF node-primitive as Scene::parse_gltf emits it (src/pathtracing/scene.rs:59-67,
+ * 185-207): transform, material and a range [index_start, index_end) of the index buffer.
+ * If world_to_local is all zeros the library inverts local_to_world itself. */
+typedef struct nb_primitive {
+  float local_to_world[16];
+  float world_to_local[16];
+  float color[4];
+  float roughness;
+  float metallic;
+  float emissive;
+  uint32_t index_start;
+  uint32_t index_end;
+} nb_primitive;
+
+/* src/pathtracing/pathtracer.rs:26-44 / pathtracing.wgsl:17-22 (16 bytes). */
+typedef struct nb_globals {
+  uint32_t sample;            /* samples accumulated so far (1-based row of the last one) */
+  float weight;               /* 1 / sample of the last dispatch */
+  uint32_t bounces;           /* default 8 */
+  float contribution_factor;  /* default 4 */
+} nb_globals;
+
+/* src/common/camera.rs:7-12.  The pass reads clip_to_world only. */
+typedef struct nb_camera {
+  float world_to_clip[16];
+  float clip_to_world[16];
+} nb_camera;
+
+/* Environment seen by rays that miss (pathtracing.wgsl:167-170).  The reference samples a
+ * BC6H cube map; this ABI takes a constant colour or an equirect RGBA32F map. */
+enum { NB_ENV_CONSTANT = 0, NB_ENV_EQUIRECT = 1 };
+typedef struct nb_env_desc {
+  uint32_t kind;
+  float color[4];          /* NB_ENV_CONSTANT */
+  const float* texels;     /* NB_ENV_EQUIRECT: height rows of width RGBA32F texels (host) */
+  uint32_t width, height;
+} nb_env_desc;
+
+typedef struct nb_scene nb_scene;
+typedef struct nb_env nb_env;
+typedef struct nb_pathtracer nb_pathtracer;
+
+typedef struct nb_scene_info {
+  uint64_t n_vertices, n_triangles, n_instances, n_blas_roots;
+  uint64_t n_blas_nodes_ref, n_tlas_nodes_ref;   /* reference-layout node counts */
+  uint64_t n_blas_nodes_gpu, n_tlas_nodes_gpu;   /* device node records (one per inner node) */
+  uint64_t device_bytes;
+  double build_ms;                               /* host BVH build time */
+} nb_scene_info;
+
+/* ---------------------------------------------------------------------------------------
+ * Library
+ * ------------------------------------------------------------------------------------- */
+int nb_version(void);
+/* Thread-local message describing the last failure on this thread ("" if none). */
+const char* nb_last_error(void);
+const char* nb_status_string(int status);
+
+/* ---------------------------------------------------------------------------------------
+ * Host-side builders (no GPU needed)
+ * ------------------------------------------------------------------------------------- */
+
+/* Sobol-Burley sample table in the reference's layout: row-major [sample][dimension set]
+ * vec4, filled with 4D Owen-scrambled Sobol points (replaces sobol_burley::sample_4d at
+ * src/pathtracing/pathtracer.rs:56-64).  out holds n_samples * n_dimsets * 4 floats. */
+int nb_sobol_burley_table(uint32_t n_samples, uint32_t n_dimsets, uint32_t seed, float* out);
+
+/* SAH BVH over one triangle list, node for node as BVHTree::append (src/pathtracing/bvh.rs:
+ * 162-190) builds it.  positions: n_vertices * 3 floats.  Writes up to nodes_capacity nodes
+ * (2 * n_triangles suffices) and the triangle-permuted index list (flatten_triangle_list,
+ * bvh.rs:106-110) into indices_out (n_indices entries). */
+int nb_bvh_build(const float* positions, size_t n_vertices, const uint32_t* indices, size_t n_indices,
+                 nb_bvh_node* nodes_out, size_t nodes_capacity, size_t* n_nodes_out, uint32_t* indices_out);
+
+/* ---------------------------------------------------------------------------------------
+ * Scenes (SceneBuffers::from_scene, src/pathtracing/scene.rs:280-453)
+ * ------------------------------------------------------------------------------------- */
+enum {
+  /* Build one BLAS per distinct index range instead of one per primitive.  The reference
+   * builds one per glTF node-primitive (scene.rs:285-299); rebuilding an already built range
+   * reproduces the same tree, so traversal results are unchanged. */
+  NB_SCENE_DEDUP_MESHES = 1u << 0,
+  /* Build and validate on the host only (no device needed, nothing uploaded): the scene can
+   * be exported and inspected but not rendered or traced. */
+  NB_SCENE_HOST_ONLY = 1u << 1
+};
+
+/* Builds BLAS + TLAS on the host (parallel over BLASes) and uploads the scene in the
+ * device layout.  indices are global vertex ids (scene.rs:173). */
+int nb_scene_create(const nb_vertex* vertices, size_t n_vertices, const uint32_t* indices, size_t n_indices,
+                    const nb_primitive* primitives, size_t n_primitives, uint32_t flags, nb_scene** out);
+
+/* Takes the reference's own prebuilt buffers (the five storage buffers of bind group 1,
+ * scene.rs:309-341 / raytracing_sw.wgsl:33-37) and uploads them in the device layout. */
+int nb_scene_create_from_bvh(const nb_bvh_node* blas, size_t n_blas, const nb_bvh_node* tlas, size_t n_tlas,
+                             const nb_instance* instances, size_t n_instances, const nb_vertex* vertices,
+                             size_t n_vertices, const uint32_t* indices, size_t n_indices, nb_scene** out);
+
+/* Copies the reference-layout buffers a scene was built from (NULL skips a buffer; sizes
+ * come from nb_scene_get_info). */
+int nb_scene_export(const nb_scene* scene, nb_bvh_node* blas, nb_bvh_node* tlas, nb_instance* instances,
+                    uint32_t* indices);
+int nb_scene_get_info(const nb_scene* scene, nb_scene_info* info);
+void nb_scene_destroy(nb_scene* scene);
+
+/* ---------------------------------------------------------------------------------------
+ * Environment
+ * ------------------------------------------------------------------------------------- */
+int nb_env_create(const nb_env_desc* desc, nb_env** out);
+void nb_env_destroy(nb_env* env);
+
+/* ---------------------------------------------------------------------------------------
+ * The pass (Pathtracer, src/pathtracing/pathtracer.rs:15-239)
+ * ------------------------------------------------------------------------------------- */
+
+/* Pathtracer::new (pathtracer.rs:51-161): allocates the RGBA32F width x height accumulation
+ * image and the Sobol table.  sobol_table may be NULL (the library builds its own,
+ * max_sample_count rows of 17 vec4, seed 0) or point to a caller-built table of
+ * sobol_rows * 17 vec4 in the reference's layout (e.g. from the sobol_burley crate).
+ * globals may be NULL (sample 0, weight 0, bounces 8, contribution_factor 4). */
+int nb_pathtracer_create(uint32_t width, uint32_t height, const nb_globals* globals, const float* sobol_table,
+                         uint32_t sobol_rows, nb_pathtracer** out);
+void nb_pathtracer_destroy(nb_pathtracer* pt);
+
+/* Pathtracer::dispatch (pathtracer.rs:225-239): adds one sample per pixel to the running
+ * mean.  Returns NB_ERR_EXHAUSTED without work once sample >= max_sample_count. */
+int nb_pathtracer_dispatch(nb_pathtracer* pt, const nb_scene* scene, const nb_camera* camera, const nb_env* env,
+                           void* stream);
+/* n_samples consecutive dispatches in one batched launch sequence; the image is identical to
+ * n_samples calls of nb_pathtracer_dispatch.  Stops early at max_sample_count. */
+int nb_pathtracer_render(nb_pathtracer* pt, const nb_scene* scene, const nb_camera* camera, const nb_env* env,
+                         uint32_t n_samples, void* stream);
+
+int nb_pathtracer_invalidate(nb_pathtracer* pt);                           /* pathtracer.rs:221-223 */
+int nb_pathtracer_resize(nb_pathtracer* pt, uint32_t width, uint32_t height); /* pathtracer.rs:208-210 */
+int nb_pathtracer_get_globals(const nb_pathtracer* pt, nb_globals* out);
+int nb_pathtracer_set_globals(nb_pathtracer* pt, const nb_globals* globals); /* pub globals (pathtracer.rs:21) */
+uint32_t nb_pathtracer_sample_count(const nb_pathtracer* pt);               /* pathtracer.rs:217-219 */
+uint32_t nb_pathtracer_max_sample_count(const nb_pathtracer* pt);           /* pathtracer.rs:23 */
+
+/* output_texture() (pathtracer.rs:204-206): device pointer of the RGBA32F image, row-major,
+ * row 0 first (the reference blit shows row 0 at the bottom of the screen). */
+int nb_pathtracer_output(const nb_pathtracer* pt, float** device_rgba, uint32_t* width, uint32_t* height);
+/* Copies the image into host memory (width * height * 4 floats) and synchronises stream. */
+int nb_pathtracer_download(const nb_pathtracer* pt, float* host_rgba, void* stream);
+/* Traversal queries issued by the last dispatch/render call (primary + extension rays) and
+ * the device status word of that call (0 = clean).  Synchronises stream. */
+int nb_pathtracer_last_stats(const nb_pathtracer* pt, uint64_t* rays, uint32_t* status, void* stream);
+
+/* Per-kernel CUDA-event timing of the pass's launches, recorded on the launch stream (the
+ * reference leaves GPU timestamps off, pathtracer.rs:229; "timer queries" is an open item of
+ * its feature list).  Off by default. */
+typedef struct nb_kernel_times {
+  double raygen_ms, trace_ms, shade_ms, accumulate_ms;
+  uint64_t raygen_launches, trace_launches, shade_launches, accumulate_launches;
+} nb_kernel_times;
+int nb_pathtracer_enable_timing(nb_pathtracer* pt, int enable);
+/* Sums the recorded launch times (synchronises stream); reset != 0 clears the record. */
+int nb_pathtracer_kernel_times(nb_pathtracer* pt, nb_kernel_times* out, int reset, void* stream);
+
+/* ---------------------------------------------------------------------------------------
+ * Traversal (the intersect_scene query, raytracing_sw.wgsl:138-250, on caller rays)
+ * ------------------------------------------------------------------------------------- */
+enum {
+  NB_TRACE_CLOSEST = 0,
+  NB_TRACE_ANY = 1u << 0 /* stop at the first accepted triangle (occlusion query) */
+};
+/* rays: n records of 8 floats (origin.xyz, unused, direction.xyz, unused) in device memory.
+ * hits: n float4 (t, u, v, triangle) with t = FLT_MAX (0x1.fffffep+127) on a miss and the
+ * triangle as a u32 bit pattern (index into the scene's permuted triangle list).
+ * instances: optional n u32 (TLAS-permuted instance index of the hit).
+ * Asynchronous: nb_scene_status() reads the device status word of the last query. */
+int nb_trace_rays(const nb_scene* scene, const float* rays, size_t n, uint32_t flags, float* hits,
+                  uint32_t* instances, void* stream);
+/* Synchronises stream and returns NB_ERR_STACK_OVERFLOW / NB_ERR_TIMEOUT if the last
+ * traversal query on this scene raised the corresponding device status bit. */
+int nb_scene_status(const nb_scene* scene, uint32_t* status, void* stream);
+/* Same query with host buffers: copies rays in and hits out inside the call and checks the
+ * status word. */
+int nb_trace_rays_host(const nb_scene* scene, const float* rays, size_t n, uint32_t flags, float* hits,
+                       uint32_t* instances, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NBOUNCE_H */

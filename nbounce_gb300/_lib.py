@@ -1,0 +1,130 @@
+"""ctypes binding of libnbounce.so (the C ABI in include/nbounce.h).
+
+Loading fails loudly when the library has not been built: there is no fallback path.
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+PKG = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(PKG, "libnbounce.so")
+
+NB_OK = 0
+NB_ERR_INVALID_ARG = 1
+NB_ERR_OOM = 2
+NB_ERR_CUDA = 3
+NB_ERR_TIMEOUT = 4
+NB_ERR_STACK_OVERFLOW = 5
+NB_ERR_NO_DEVICE = 6
+NB_ERR_EXHAUSTED = 7
+
+NB_SCENE_DEDUP_MESHES = 1
+NB_SCENE_HOST_ONLY = 2
+NB_ENV_CONSTANT = 0
+NB_ENV_EQUIRECT = 1
+NB_TRACE_CLOSEST = 0
+NB_TRACE_ANY = 1
+
+VERTEX_DTYPE = np.dtype([("pos", "<f4", 3), ("u", "<f4"), ("nrm", "<f4", 3), ("v", "<f4"), ("tan", "<f4", 4)])
+NODE_DTYPE = np.dtype([("min", "<f4", 3), ("start", "<u4"), ("max", "<f4", 3), ("end", "<u4")])
+INSTANCE_DTYPE = np.dtype([("w2l", "<f4", 16), ("l2w", "<f4", 16), ("color", "<f4", 4), ("roughness", "<f4"),
+                           ("metallic", "<f4"), ("emissive", "<f4"), ("node", "<u4")])
+PRIMITIVE_DTYPE = np.dtype([("l2w", "<f4", 16), ("w2l", "<f4", 16), ("color", "<f4", 4), ("roughness", "<f4"),
+                            ("metallic", "<f4"), ("emissive", "<f4"), ("index_start", "<u4"), ("index_end", "<u4")])
+
+
+class NbGlobals(C.Structure):
+    _fields_ = [("sample", C.c_uint32), ("weight", C.c_float), ("bounces", C.c_uint32),
+                ("contribution_factor", C.c_float)]
+
+
+class NbCamera(C.Structure):
+    _fields_ = [("world_to_clip", C.c_float * 16), ("clip_to_world", C.c_float * 16)]
+
+
+class NbEnvDesc(C.Structure):
+    _fields_ = [("kind", C.c_uint32), ("color", C.c_float * 4), ("texels", C.c_void_p), ("width", C.c_uint32),
+                ("height", C.c_uint32)]
+
+
+class NbSceneInfo(C.Structure):
+    _fields_ = [("n_vertices", C.c_uint64), ("n_triangles", C.c_uint64), ("n_instances", C.c_uint64),
+                ("n_blas_roots", C.c_uint64), ("n_blas_nodes_ref", C.c_uint64), ("n_tlas_nodes_ref", C.c_uint64),
+                ("n_blas_nodes_gpu", C.c_uint64), ("n_tlas_nodes_gpu", C.c_uint64), ("device_bytes", C.c_uint64),
+                ("build_ms", C.c_double)]
+
+
+class NbKernelTimes(C.Structure):
+    _fields_ = [("raygen_ms", C.c_double), ("trace_ms", C.c_double), ("shade_ms", C.c_double),
+                ("accumulate_ms", C.c_double), ("raygen_launches", C.c_uint64), ("trace_launches", C.c_uint64),
+                ("shade_launches", C.c_uint64), ("accumulate_launches", C.c_uint64)]
+
+
+class NbError(RuntimeError):
+    def __init__(self, status, message):
+        super().__init__(f"{message} (status {status})")
+        self.status = status
+
+
+_lib = None
+
+
+def lib():
+    """Loads libnbounce.so; raises if it is missing (no fallback)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        raise RuntimeError(f"{LIB_PATH} is not built; run nbounce_gb300.build.build() first")
+    L = C.CDLL(LIB_PATH)
+    vp, u32, u64, i32, sz = C.c_void_p, C.c_uint32, C.c_uint64, C.c_int, C.c_size_t
+    sig = {
+        "nb_version": ([], i32),
+        "nb_last_error": ([], C.c_char_p),
+        "nb_status_string": ([i32], C.c_char_p),
+        "nb_sobol_burley_table": ([u32, u32, u32, vp], i32),
+        "nb_bvh_build": ([vp, sz, vp, sz, vp, sz, vp, vp], i32),
+        "nb_scene_create": ([vp, sz, vp, sz, vp, sz, u32, vp], i32),
+        "nb_scene_create_from_bvh": ([vp, sz, vp, sz, vp, sz, vp, sz, vp, sz, vp], i32),
+        "nb_scene_export": ([vp, vp, vp, vp, vp], i32),
+        "nb_scene_get_info": ([vp, vp], i32),
+        "nb_scene_status": ([vp, vp, vp], i32),
+        "nb_scene_destroy": ([vp], None),
+        "nb_env_create": ([vp, vp], i32),
+        "nb_env_destroy": ([vp], None),
+        "nb_pathtracer_create": ([u32, u32, vp, vp, u32, vp], i32),
+        "nb_pathtracer_destroy": ([vp], None),
+        "nb_pathtracer_dispatch": ([vp, vp, vp, vp, vp], i32),
+        "nb_pathtracer_render": ([vp, vp, vp, vp, u32, vp], i32),
+        "nb_pathtracer_invalidate": ([vp], i32),
+        "nb_pathtracer_resize": ([vp, u32, u32], i32),
+        "nb_pathtracer_get_globals": ([vp, vp], i32),
+        "nb_pathtracer_set_globals": ([vp, vp], i32),
+        "nb_pathtracer_sample_count": ([vp], u32),
+        "nb_pathtracer_max_sample_count": ([vp], u32),
+        "nb_pathtracer_output": ([vp, vp, vp, vp], i32),
+        "nb_pathtracer_download": ([vp, vp, vp], i32),
+        "nb_pathtracer_last_stats": ([vp, vp, vp, vp], i32),
+        "nb_pathtracer_enable_timing": ([vp, i32], i32),
+        "nb_pathtracer_kernel_times": ([vp, vp, i32, vp], i32),
+        "nb_trace_rays": ([vp, vp, sz, u32, vp, vp, vp], i32),
+        "nb_trace_rays_host": ([vp, vp, sz, u32, vp, vp, vp], i32),
+    }
+    for name, (args, res) in sig.items():
+        f = getattr(L, name)
+        f.argtypes = args
+        f.restype = res
+    _lib = L
+    return L
+
+
+def check(status):
+    if status != NB_OK:
+        msg = lib().nb_last_error().decode(errors="replace")
+        raise NbError(status, msg or lib().nb_status_string(status).decode())
+    return status
+
+
+def ptr(a):
+    return None if a is None else C.c_void_p(a.ctypes.data)

@@ -1,0 +1,547 @@
+// CUDA kernels of the nBounce path-tracing pass for sm_103a.
+//
+// The reference runs one WGSL invocation per pixel that loops over bounces with the whole
+// traversal inline (pathtracing.wgsl:161-260).  Here the pass is a wavefront:
+//   raygen      one path per (pixel, sample) of a batch: Cranley-Patterson-rotated Sobol
+//               jitter and generate_ray (pathtracing.wgsl:27-41, 245-255)
+//   trace       persistent warps pull 32-ray chunks with one atomic each and run the
+//               two-level stack traversal (raytracing_sw.wgsl:176-319) on the device layout
+//   shade       hit attributes (raytracing_sw.wgsl:138-173), env/emission termination, lobe
+//               choice, VNDF / cosine sampling, Russian roulette (pathtracing.wgsl:161-241);
+//               survivors are appended to the next bounce's queue with warp-aggregated atomics
+//   accumulate  running mean over the batch's samples in sample order (pathtracing.wgsl:258)
+// so traversal runs in a lean kernel at full occupancy and the path state lives in HBM.
+//
+// Traversal differs from the reference in two work-saving ways that leave results unchanged
+// except for near-ties: the current closest hit prunes BLAS nodes (the reference restarts
+// each BLAS from NO_HIT, raytracing_sw.wgsl:255) and one stack serves both levels.
+
+#include <algorithm>
+#include <cstdint>
+
+#include "nb_device.cuh"
+#include "nb_launch.h"
+
+namespace nbd {
+
+using nb::CameraParams;
+using nb::kMaxBounceSlots;
+using nb::PathBatch;
+
+constexpr int kStackSize = 64;
+constexpr uint32_t kIterationCap = 1u << 22;
+
+__device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
+
+// slab test (raytracing_sw.wgsl:81-89)
+__device__ __forceinline__ float slab(V3 ro, V3 rinv, float mnx, float mxx, float mny, float mxy, float mnz,
+                                      float mxz) {
+  float tminx = (mnx - ro.x) * rinv.x, tmaxx = (mxx - ro.x) * rinv.x;
+  float tminy = (mny - ro.y) * rinv.y, tmaxy = (mxy - ro.y) * rinv.y;
+  float tminz = (mnz - ro.z) * rinv.z, tmaxz = (mxz - ro.z) * rinv.z;
+  float t1x = fminf(tminx, tmaxx), t1y = fminf(tminy, tmaxy), t1z = fminf(tminz, tmaxz);
+  float t2x = fmaxf(tminx, tmaxx), t2y = fmaxf(tminy, tmaxy), t2z = fmaxf(tminz, tmaxz);
+  float tn = fmaxf(t1x, fmaxf(t1y, t1z));
+  float tf = fminf(t2x, fminf(t2y, t2z));
+  return (tn <= tf && tf >= 0.0f) ? tn : kNoHit;
+}
+
+struct Hit {
+  float t, u, v;
+  uint32_t tri, inst;
+};
+
+struct TraceCounters {
+  uint32_t nodes, tris, insts;
+};
+
+// Closest (or any) hit of one world-space ray.  Returns the status bits it raised.
+template <bool kAny, bool kStats>
+__device__ uint32_t trace_ray(const DevScene& s, V3 wo, V3 wd, Hit* out, TraceCounters* cnt) {
+  Hit h;
+  h.t = kNoHit;
+  h.u = h.v = 0.0f;
+  h.tri = 0xFFFFFFFFu;
+  h.inst = 0xFFFFFFFFu;
+  uint32_t status = 0;
+  if (!s.has_tlas) {
+    *out = h;
+    return 0;
+  }
+  const V3 winv = rcp3(wd);
+  V3 ro = wo, rd = wd, rinv = winv;
+  uint2 stack[kStackSize];
+  int sp = 0;
+  bool in_blas = false;
+  uint32_t inst_cur = 0, inst_end = 0, cur_inst = 0;
+  int blas_base = 0;
+
+  auto push = [&](uint32_t ref, float d) {
+    if (sp < kStackSize) {
+      stack[sp] = make_uint2(ref, __float_as_uint(d));
+      ++sp;
+    } else {
+      status |= kStatusStackOverflow;
+    }
+  };
+  // enter the BLAS of instance j: transform the world ray (raytracing_sw.wgsl:202-206)
+  auto start_instance = [&](uint32_t j) {
+    const float4* it = s.inst_trace + 4 * (size_t)j;
+    float4 r0 = ld4(it), r1 = ld4(it + 1), r2 = ld4(it + 2);
+    uint32_t root = __float_as_uint(ld4(it + 3).x);
+    ro = V3{r0.x * wo.x + r0.y * wo.y + r0.z * wo.z + r0.w * 1.0f,
+            r1.x * wo.x + r1.y * wo.y + r1.z * wo.z + r1.w * 1.0f,
+            r2.x * wo.x + r2.y * wo.y + r2.z * wo.z + r2.w * 1.0f};
+    rd = V3{r0.x * wd.x + r0.y * wd.y + r0.z * wd.z, r1.x * wd.x + r1.y * wd.y + r1.z * wd.z,
+            r2.x * wd.x + r2.y * wd.y + r2.z * wd.z};
+    rinv = rcp3(rd);
+    cur_inst = j;
+    float4 lo = ld4(s.blas_roots + 2 * (size_t)root), hi = ld4(s.blas_roots + 2 * (size_t)root + 1);
+    float d = slab(ro, rinv, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
+    if (kStats) { cnt->nodes += 1; cnt->insts += 1; }
+    if (d < h.t) push(__float_as_uint(lo.w), d);
+  };
+
+  {
+    float4 lo = s.tlas_root_lo, hi = s.tlas_root_hi;
+    float d = slab(wo, winv, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
+    if (kStats) cnt->nodes += 1;
+    if (d < h.t) push(__float_as_uint(lo.w), d);
+  }
+  uint32_t iter = 0;
+  while (true) {
+    if (++iter > kIterationCap) {
+      status |= kStatusIterationCap;
+      break;
+    }
+    if (in_blas && sp == blas_base) {
+      if (inst_cur < inst_end) {
+        start_instance(inst_cur++);
+        continue;
+      }
+      in_blas = false;
+      ro = wo; rd = wd; rinv = winv;
+    }
+    if (sp == 0) break;
+    --sp;
+    uint2 e = stack[sp];
+    if (__uint_as_float(e.y) >= h.t) continue;
+    const uint32_t ref = e.x;
+    if (ref & kLeafBit) {
+      const uint32_t first = ref & ~kLeafBit;
+      if (!in_blas) {
+        // TLAS leaf: instances [first, first + n) one after the other (raytracing_sw.wgsl:200-217)
+        uint32_t n = __float_as_uint(ld4(s.inst_trace + 4 * (size_t)first + 3).y);
+        inst_cur = first;
+        inst_end = first + n;
+        in_blas = true;
+        blas_base = sp;
+        start_instance(inst_cur++);
+      } else {
+        // BLAS leaf: Moller-Trumbore over the leaf's triangles (raytracing_sw.wgsl:274-286)
+        const float4* tp = s.tris + 3 * (size_t)first;
+        float4 a = ld4(tp);
+        const uint32_t n = __float_as_uint(a.w);
+        for (uint32_t k = 0; k < n; ++k) {
+          if (k) a = ld4(tp + 3 * k);
+          float4 b = ld4(tp + 3 * k + 1), c = ld4(tp + 3 * k + 2);
+          if (kStats) cnt->tris += 1;
+          V3 e1 = xyz(b), e2 = xyz(c);
+          V3 hv = cross(rd, e2);
+          float det = dot(e1, hv);
+          if (det < kEps) continue;
+          float inv_det = 1.0f / det;
+          V3 sv = ro - xyz(a);
+          float u = inv_det * dot(sv, hv);
+          if (u < 0.0f || u > 1.0f) continue;
+          V3 q = cross(sv, e1);
+          float v = inv_det * dot(rd, q);
+          if (v < 0.0f || u + v > 1.0f) continue;
+          float t = inv_det * dot(e2, q);
+          if (t < kBias) continue;
+          if (t < h.t) {
+            h.t = t; h.u = u; h.v = v;
+            h.tri = first + k;
+            h.inst = cur_inst;
+            if (kAny) {
+              *out = h;
+              return status;
+            }
+          }
+        }
+      }
+    } else {
+      // inner node: test both children, push far then near (raytracing_sw.wgsl:218-247)
+      const float4* np = (in_blas ? s.blas_nodes : s.tlas_nodes) + 4 * (size_t)ref;
+      float4 q0 = ld4(np), q1 = ld4(np + 1), q2 = ld4(np + 2), q3 = ld4(np + 3);
+      float dl = slab(ro, rinv, q0.x, q0.y, q0.z, q0.w, q2.x, q2.y);
+      float dr = slab(ro, rinv, q1.x, q1.y, q1.z, q1.w, q2.z, q2.w);
+      if (kStats) cnt->nodes += 2;
+      uint32_t lref = __float_as_uint(q3.x), rref = __float_as_uint(q3.y);
+      uint32_t fref = lref, nref = rref;
+      float fd = dl, nd = dr;
+      if (dl < dr) { fref = rref; fd = dr; nref = lref; nd = dl; }
+      if (fd < h.t) push(fref, fd);
+      if (nd < h.t) push(nref, nd);
+    }
+  }
+  *out = h;
+  return status;
+}
+
+// ------------------------------------------------------------------------------------------
+// traversal-only query (nb_trace_rays)
+// ------------------------------------------------------------------------------------------
+template <bool kAny>
+__global__ void __launch_bounds__(128) k_trace_rays(DevScene s, const float4* __restrict__ rays, uint32_t n,
+                                                     float4* __restrict__ hits, uint32_t* __restrict__ inst,
+                                                     uint32_t* __restrict__ fetch, uint32_t* __restrict__ status) {
+  const int lane = threadIdx.x & 31;
+  uint32_t st = 0;
+  while (true) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(fetch, 32u);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (base >= n) break;
+    uint32_t i = base + lane;
+    if (i < n) {
+      float4 o = __ldg(rays + 2 * (size_t)i), d = __ldg(rays + 2 * (size_t)i + 1);
+      Hit h;
+      TraceCounters c;
+      st |= trace_ray<kAny, false>(s, xyz(o), xyz(d), &h, &c);
+      hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
+      if (inst) inst[i] = h.inst;
+    }
+  }
+  if (st) atomicOr(status, st);
+}
+
+// ------------------------------------------------------------------------------------------
+// wavefront path tracer
+// ------------------------------------------------------------------------------------------
+__device__ __forceinline__ float4 sobol_read(const float4* table, uint32_t n_entries, uint32_t idx) {
+  return idx < n_entries ? __ldg(table + idx) : make_float4(0.f, 0.f, 0.f, 0.f);  // robust buffer access
+}
+
+// generate_ray (pathtracing.wgsl:27-41)
+__device__ __forceinline__ void generate_ray(uint32_t x, uint32_t y, uint32_t W, uint32_t H, float rx, float ry,
+                                             const CameraParams& cam, V3* o, V3* d) {
+  float uvx = 2.0f * ((float)x + rx) / (float)W - 1.0f;
+  float uvy = 2.0f * ((float)y + ry) / (float)H - 1.0f;
+  const float* m = cam.c2w;
+  V3 pos = V3{m[12], m[13], m[14]} / m[15];
+  float cx = -uvx, cy = -uvy, cz = -1.0f, cw = 1.0f;
+  float wd[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) wd[r] = m[r] * cx + m[4 + r] * cy + m[8 + r] * cz + m[12 + r] * cw;
+  *o = pos;
+  *d = pos - V3{wd[0], wd[1], wd[2]} / wd[3];
+}
+
+__global__ void __launch_bounds__(256) k_raygen(PathBatch pb, CameraParams cam) {
+  const uint32_t n = pb.n_paths;
+  if (blockIdx.x == 0 && threadIdx.x < kMaxBounceSlots) {
+    pb.counts[threadIdx.x] = threadIdx.x == 0 ? n : 0u;
+    pb.fetch[threadIdx.x] = 0u;
+  }
+  for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
+    uint32_t pix = p % pb.npix;
+    uint32_t sample = pb.first_sample + p / pb.npix;
+    uint32_t x = pix % pb.width, y = pix / pb.width;
+    float4 shift = hash4f(x, y);
+    float4 sb = sobol_read(pb.sobol, pb.sobol_entries, sample * kLdsStride);
+    float jx = fract(sb.x + shift.x), jy = fract(sb.y + shift.y);
+    V3 o, d;
+    generate_ray(x, y, pb.width, pb.height, jx, jy, cam, &o, &d);
+    pb.q_o[0][p] = make_float4(o.x, o.y, o.z, __uint_as_float(p));
+    pb.q_d[0][p] = make_float4(d.x, d.y, d.z, 0.0f);
+    pb.q_t[0][p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+    pb.radiance[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  }
+}
+
+__global__ void __launch_bounds__(128) k_trace_wave(DevScene s, PathBatch pb, uint32_t bounce,
+                                                    unsigned long long* __restrict__ ray_total) {
+  const uint32_t n = pb.counts[bounce];
+  const float4* __restrict__ qo = (bounce & 1) ? pb.q_o[1] : pb.q_o[0];
+  const float4* __restrict__ qd = (bounce & 1) ? pb.q_d[1] : pb.q_d[0];
+  const int lane = threadIdx.x & 31;
+  uint32_t st = 0;
+  while (true) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(pb.fetch + bounce, 32u);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (base >= n) break;
+    uint32_t i = base + lane;
+    if (i < n) {
+      float4 o = qo[i], d = qd[i];
+      Hit h;
+      TraceCounters c;
+      st |= trace_ray<false, false>(s, xyz(o), xyz(d), &h, &c);
+      pb.hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
+      pb.hit_inst[i] = h.inst;
+    }
+  }
+  if (st) atomicOr(pb.status, st);
+  if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(ray_total, (unsigned long long)n);
+}
+
+// equirect lookup, evaluated in binary64 (the oracle's definition): u = atan2(x, -z)/(2 pi) + 0.5,
+// v = acos(y)/pi of the normalised direction, bilinear with wrap in u and clamp in v
+__device__ V3 env_lookup(const DevEnv& env, V3 dir) {
+  if (env.kind == kEnvConstant) return V3{env.r, env.g, env.b};
+  double dx = dir.x, dy = dir.y, dz = dir.z;
+  double l = sqrt(dx * dx + dy * dy + dz * dz);
+  dx /= l; dy /= l; dz /= l;
+  const double kPiD = 3.14159265358979323846;
+  double u = atan2(dx, -dz) / (2.0 * kPiD) + 0.5;
+  double v = acos(fmax(-1.0, fmin(1.0, dy))) / kPiD;
+  double fx = u * env.width - 0.5, fy = v * env.height - 0.5;
+  double x0 = floor(fx), y0 = floor(fy);
+  double tx = fx - x0, ty = fy - y0;
+  long W = env.width, H = env.height;
+  long xi0 = (((long)x0 % W) + W) % W, xi1 = (((long)x0 + 1) % W + W) % W;
+  long yi0 = (long)y0 < 0 ? 0 : ((long)y0 > H - 1 ? H - 1 : (long)y0);
+  long yi1 = (long)y0 + 1 < 0 ? 0 : ((long)y0 + 1 > H - 1 ? H - 1 : (long)y0 + 1);
+  float4 t00 = __ldg(env.texels + yi0 * W + xi0), t10 = __ldg(env.texels + yi0 * W + xi1);
+  float4 t01 = __ldg(env.texels + yi1 * W + xi0), t11 = __ldg(env.texels + yi1 * W + xi1);
+  double c0 = ((double)t00.x * (1 - tx) + (double)t10.x * tx) * (1 - ty) + ((double)t01.x * (1 - tx) + (double)t11.x * tx) * ty;
+  double c1 = ((double)t00.y * (1 - tx) + (double)t10.y * tx) * (1 - ty) + ((double)t01.y * (1 - tx) + (double)t11.y * tx) * ty;
+  double c2 = ((double)t00.z * (1 - tx) + (double)t10.z * tx) * (1 - ty) + ((double)t01.z * (1 - tx) + (double)t11.z * tx) * ty;
+  return V3{(float)c0, (float)c1, (float)c2};
+}
+
+// sample_vndf_iso (pathtracing.wgsl:68-98)
+__device__ __forceinline__ V3 sample_vndf_iso(float r0, float r1, V3 wi, float alpha, V3 n) {
+  if (alpha == 0.0f) return n;
+  V3 wi_z = n * dot(wi, n);
+  V3 wi_xy = wi - wi_z;
+  V3 wiStd = normalize(wi_z - alpha * wi_xy);
+  float wiStd_z = dot(wiStd, n);
+  float phi = (2.0f * r0 - 1.0f) * kPi;
+  float z = (1.0f - r1) * (1.0f + wiStd_z) - wiStd_z;
+  float sinTheta = sqrtf(fminf(fmaxf(1.0f - z * z, 0.0f), 1.0f));
+  float sp, cp;
+  nb_sincos(phi, &sp, &cp);
+  V3 cStd{sinTheta * cp, sinTheta * sp, z};
+  V3 wr = n + V3{0.0f, 0.0f, 1.0f};
+  float safe_wrz = fmaxf(wr.z, 1e-6f);
+  V3 c = dot(wr, cStd) * wr / safe_wrz - cStd;
+  V3 wmStd = c + wiStd;
+  V3 wmStd_z = n * dot(n, wmStd);
+  V3 wmStd_xy = wmStd_z - wmStd;
+  return normalize(wmStd_z + alpha * wmStd_xy);
+}
+
+__device__ __forceinline__ V3 F_schlick(float hdotv, V3 r0) {  // pathtracing.wgsl:113-115
+  float p = pow5(1.0f - hdotv);
+  return r0 + (V3{1.0f, 1.0f, 1.0f} - r0) * p;
+}
+__device__ __forceinline__ float lambda_tr(float ndotv, float alpha2) {  // pathtracing.wgsl:119-125
+  float cos2 = ndotv * ndotv;
+  float sin2 = 1.0f - cos2;
+  float tan2 = sin2 / cos2;
+  return (-1.0f + sqrtf(1.0f + alpha2 * tan2)) / 2.0f;
+}
+
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool active) {
+  const uint32_t mask = __ballot_sync(0xFFFFFFFFu, active);
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(mask) - 1;
+  uint32_t base = 0;
+  if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+  base = __shfl_sync(0xFFFFFFFFu, base, leader < 0 ? 0 : leader);
+  return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+__global__ void __launch_bounds__(256) k_shade(DevScene s, DevEnv env, PathBatch pb, uint32_t bounce,
+                                               uint32_t bounces, float cf) {
+  const uint32_t n = pb.counts[bounce];
+  const bool odd = (bounce & 1) != 0;
+  const float4* __restrict__ in_o = odd ? pb.q_o[1] : pb.q_o[0];
+  const float4* __restrict__ in_d = odd ? pb.q_d[1] : pb.q_d[0];
+  const float4* __restrict__ in_t = odd ? pb.q_t[1] : pb.q_t[0];
+  float4* __restrict__ out_o = odd ? pb.q_o[0] : pb.q_o[1];
+  float4* __restrict__ out_d = odd ? pb.q_d[0] : pb.q_d[1];
+  float4* __restrict__ out_t = odd ? pb.q_t[0] : pb.q_t[1];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  // whole warps iterate together so warp_append sees converged warps
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    bool cont = false;
+    float4 next_o = make_float4(0.f, 0.f, 0.f, 0.f), next_d = next_o, next_t = next_o;
+    if (i < n) {
+      float4 O = in_o[i], D = in_d[i], Tq = in_t[i], H = pb.hits[i];
+      const uint32_t id = __float_as_uint(O.w);
+      V3 T = xyz(Tq);
+      V3 rdir = xyz(D);
+      if (H.x == kNoHit) {
+        V3 L = T * env_lookup(env, rdir);
+        pb.radiance[id] = make_float4(L.x, L.y, L.z, 0.0f);
+      } else {
+        const uint32_t inst = pb.hit_inst[i];
+        const float4* sh = s.inst_shade + 6 * (size_t)inst;
+        float4 c0 = ld4(sh), c1 = ld4(sh + 1), c2 = ld4(sh + 2);
+        float4 l0 = ld4(sh + 3), l1 = ld4(sh + 4), l2 = ld4(sh + 5);
+        V3 color{c0.w, c1.w, c2.w};
+        if (l2.w > 0.0f) {  // EMISSIVE (raytracing_sw.wgsl:168-170, pathtracing.wgsl:172-174)
+          V3 L = T * color;
+          pb.radiance[id] = make_float4(L.x, L.y, L.z, 0.0f);
+        } else {
+          // hit attributes (raytracing_sw.wgsl:146-158)
+          const uint32_t tri = __float_as_uint(H.w);
+          const uint32_t i0 = __ldg(s.tri_idx + 3 * (size_t)tri), i1 = __ldg(s.tri_idx + 3 * (size_t)tri + 1),
+                         i2 = __ldg(s.tri_idx + 3 * (size_t)tri + 2);
+          float4 a0 = ld4(s.vattr + 2 * (size_t)i0), a1 = ld4(s.vattr + 2 * (size_t)i1), a2 = ld4(s.vattr + 2 * (size_t)i2);
+          float4 b0 = ld4(s.vattr + 2 * (size_t)i0 + 1), b1 = ld4(s.vattr + 2 * (size_t)i1 + 1),
+                 b2 = ld4(s.vattr + 2 * (size_t)i2 + 1);
+          const float u = H.y, v = H.z;
+          const float w0 = 1.0f - u - v;
+          V3 ln = xyz(a0) * w0 + xyz(a1) * u + xyz(a2) * v;
+          V3 lt = xyz(b0) * w0 + xyz(b1) * u + xyz(b2) * v;
+          V3 nrm{dot(xyz(c0), ln), dot(xyz(c1), ln), dot(xyz(c2), ln)};
+          V3 tng{dot(xyz(l0), lt), dot(xyz(l1), lt), dot(xyz(l2), lt)};
+          V3 pos = xyz(O) + H.x * rdir;
+
+          const uint32_t pix = id % pb.npix;
+          const uint32_t sample = pb.first_sample + id / pb.npix;
+          const float4 shift = hash4f(pix % pb.width, pix / pb.width);
+          const float roughness = l0.w, metallic = l1.w;
+          const float alpha = roughness * roughness;
+          const float alpha2 = alpha * alpha;
+          V3 nn = normalize(nrm);
+          const uint32_t sb = sample * kLdsStride + 1u + bounce * kLdsPerBounce;
+          float4 s0 = sobol_read(pb.sobol, pb.sobol_entries, sb);
+          float4 s1 = sobol_read(pb.sobol, pb.sobol_entries, sb + 1u);
+          s0 = make_float4(fract(s0.x + shift.x), fract(s0.y + shift.y), fract(s0.z + shift.z), 0.0f);
+          s1 = make_float4(0.0f, fract(s1.y + shift.y), fract(s1.z + shift.z), 0.0f);
+          V3 wo = normalize(-rdir);
+          float cosThetaO = dot(wo, nn);
+          V3 wi;
+          V3 F0 = V3{0.04f, 0.04f, 0.04f} * (1.0f - metallic) + color * metallic;
+          float specular_weight = luminance(F_schlick(dot(wo, nn), F0));
+          float diffuse_weight = (1.0f - metallic) * luminance(color);
+          float p_specular = specular_weight / (specular_weight + diffuse_weight);
+          float p_diffuse = 1.0f - p_specular;
+          if (s0.x < p_specular) {
+            V3 wm = sample_vndf_iso(s0.y, s0.z, wo, alpha, nn);
+            V3 ni = -wo;
+            wi = ni - (2.0f * dot(wm, ni)) * wm;  // reflect(-wo, wm)
+            float cosThetaD = dot(wo, wm);
+            float cosThetaI = dot(wi, nn);
+            V3 F = F_schlick(cosThetaD, F0);
+            float LambdaL = lambda_tr(cosThetaI, alpha2);
+            float LambdaV = lambda_tr(cosThetaO, alpha2);
+            V3 spec = F * (1.0f + LambdaV) / (1.0f + LambdaL + LambdaV);
+            T = T * (spec / p_specular);
+          } else {
+            V3 nt = normalize(tng - dot(tng, nn) * nn);  // build_tbn (common.wgsl:55-59)
+            V3 bt = cross(nn, nt);
+            float phi = kTwoPi * s1.y;
+            float sinT = sqrtf(1.0f - s1.z);
+            float cosT = sqrtf(s1.z);
+            float sp, cp;
+            nb_sincos(phi, &sp, &cp);
+            V3 ls{cp * sinT, sp * sinT, cosT};
+            wi = nt * ls.x + bt * ls.y + nn * ls.z;
+            V3 wm = normalize(wi + wo);
+            float cosThetaD = dot(wi, wm);
+            float cosThetaI = dot(wi, nn);
+            float FD90 = 0.5f + 2.0f * alpha * pow2(cosThetaD);
+            float response = (1.0f + (FD90 - 1.0f) * pow5(1.0f - cosThetaI)) * (1.0f + (FD90 - 1.0f) * pow5(1.0f - cosThetaO));
+            V3 diffuse = (1.0f - metallic) * color * response;
+            T = T * (diffuse / p_diffuse);
+          }
+          // Russian roulette (pathtracing.wgsl:225-236)
+          float p_continue = fminf(1.0f - pow8((float)bounce / (float)bounces), 1.0f);
+          p_continue = p_continue * fminf(luminance(T) * cf, 1.0f);
+          if (s0.z < p_continue && bounce < bounces) {
+            T = T / p_continue;
+            cont = true;
+            next_o = make_float4(pos.x, pos.y, pos.z, O.w);
+            next_d = make_float4(wi.x, wi.y, wi.z, 0.0f);
+            next_t = make_float4(T.x, T.y, T.z, 0.0f);
+          }
+        }
+      }
+    }
+    const uint32_t slot = warp_append(pb.counts + bounce + 1, cont);
+    if (cont) {
+      out_o[slot] = next_o;
+      out_d[slot] = next_d;
+      out_t[slot] = next_t;
+    }
+  }
+}
+
+// running mean in sample order: out = mix(out, L_k, 1/k) (pathtracing.wgsl:246-260)
+__global__ void __launch_bounds__(256) k_accumulate(PathBatch pb, float4* __restrict__ out, uint32_t n_samples) {
+  for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < pb.npix; pix += gridDim.x * blockDim.x) {
+    float4 c = out[pix];
+    for (uint32_t k = 0; k < n_samples; ++k) {
+      const float w = 1.0f / (float)(pb.first_sample + k);
+      const float4 L = pb.radiance[(size_t)k * pb.npix + pix];
+      c.x = c.x * (1.0f - w) + L.x * w;
+      c.y = c.y * (1.0f - w) + L.y * w;
+      c.z = c.z * (1.0f - w) + L.z * w;
+    }
+    out[pix] = make_float4(c.x, c.y, c.z, 1.0f);
+  }
+}
+
+}  // namespace nbd
+
+// ------------------------------------------------------------------------------------------
+// launchers
+// ------------------------------------------------------------------------------------------
+namespace nb {
+
+static int blocks_for(const void* kernel, int threads, int sms) {
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, threads, 0) != cudaSuccess || per_sm < 1)
+    per_sm = 1;
+  return per_sm * sms;
+}
+
+cudaError_t launch_trace_rays(const nbd::DevScene& s, const float* rays, uint32_t n, bool any, float* hits,
+                              uint32_t* inst, uint32_t* fetch, uint32_t* status, int sms, cudaStream_t st) {
+  cudaError_t e = cudaMemsetAsync(fetch, 0, sizeof(uint32_t), st);
+  if (e != cudaSuccess) return e;
+  if (n == 0) return cudaSuccess;
+  if (any) {
+    int g = blocks_for((const void*)nbd::k_trace_rays<true>, 128, sms);
+    nbd::k_trace_rays<true><<<g, 128, 0, st>>>(s, (const float4*)rays, n, (float4*)hits, inst, fetch, status);
+  } else {
+    int g = blocks_for((const void*)nbd::k_trace_rays<false>, 128, sms);
+    nbd::k_trace_rays<false><<<g, 128, 0, st>>>(s, (const float4*)rays, n, (float4*)hits, inst, fetch, status);
+  }
+  return cudaGetLastError();
+}
+
+cudaError_t launch_raygen(const PathBatch& pb, const CameraParams& cam, int sms, cudaStream_t st) {
+  int g = (int)std::min<uint64_t>((pb.n_paths + 255) / 256, (uint64_t)sms * 16);
+  nbd::k_raygen<<<g < 1 ? 1 : g, 256, 0, st>>>(pb, cam);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_trace_wave(const nbd::DevScene& s, const PathBatch& pb, uint32_t bounce,
+                              unsigned long long* ray_total, int sms, cudaStream_t st) {
+  static const int grid = blocks_for((const void*)nbd::k_trace_wave, 128, sms);
+  nbd::k_trace_wave<<<grid, 128, 0, st>>>(s, pb, bounce, ray_total);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shade(const nbd::DevScene& s, const nbd::DevEnv& env, const PathBatch& pb, uint32_t bounce,
+                         uint32_t bounces, float cf, int sms, cudaStream_t st) {
+  static const int grid = blocks_for((const void*)nbd::k_shade, 256, sms);
+  nbd::k_shade<<<grid, 256, 0, st>>>(s, env, pb, bounce, bounces, cf);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_accumulate(const PathBatch& pb, uint32_t n_samples, float* out, int sms, cudaStream_t st) {
+  int g = (int)std::min<uint64_t>((pb.npix + 255) / 256, (uint64_t)sms * 16);
+  nbd::k_accumulate<<<g < 1 ? 1 : g, 256, 0, st>>>(pb, (float4*)out, n_samples);
+  return cudaGetLastError();
+}
+
+}  // namespace nb

@@ -1,0 +1,110 @@
+"""Traversal parity: the CUDA intersect_scene query against the oracle's restatement of
+raytracing_sw.wgsl on the same seeded rays and the same trees.
+
+Bar (from the pass's parity spec): hit triangle/instance ids bit-exact except documented
+near-ties; t and barycentrics within 1e-5 relative.  A near-tie is a ray whose two answers
+lie within 1e-5 relative in t (two triangles the ray meets at the same distance, e.g. on a
+shared edge, resolved by a different traversal order).
+"""
+import numpy as np
+import pytest
+
+import nbounce_gb300 as nb
+from nbounce_gb300 import scenes
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+
+NO_HIT = np.float32(3.4028234663852886e38)
+REL_TOL = 1e-5
+
+
+def compare_hits(gpu_hits, gpu_inst, perm_indices, ref_f, ref_u, max_tie_frac=1e-3):
+    g_t = gpu_hits[:, 0]
+    r_t = ref_f[:, 0]
+    g_hit = g_t != NO_HIT
+    r_hit = r_t != NO_HIT
+    tri = gpu_hits[:, 3].view(np.uint32)
+    idx3 = perm_indices.reshape(-1, 3)
+    g_ids = np.full((len(g_t), 3), 0xFFFFFFFF, np.uint32)
+    g_ids[g_hit] = idx3[tri[g_hit]]
+    same = (g_hit == r_hit)
+    both = g_hit & r_hit
+    same[both] = np.all(g_ids[both] == ref_u[both, 1:], axis=1) & (gpu_inst[both] == ref_u[both, 0])
+    mism = ~same
+    # every mismatch must be a near-tie
+    t_a = np.where(g_hit, g_t, np.inf).astype(np.float64)
+    t_b = np.where(r_hit, r_t, np.inf).astype(np.float64)
+    with np.errstate(invalid="ignore"):
+        tie = np.abs(t_a - t_b) <= REL_TOL * np.minimum(t_a, t_b)
+    assert np.all(tie[mism]), f"{int(np.sum(mism & ~tie))} non-tie mismatches"
+    assert mism.mean() <= max_tie_frac, f"near-tie fraction {mism.mean():.2e}"
+    ok = both & same
+    np.testing.assert_allclose(g_t[ok], r_t[ok], rtol=REL_TOL)
+    np.testing.assert_allclose(gpu_hits[ok, 1:3], ref_f[ok, 1:3], rtol=REL_TOL, atol=REL_TOL)
+    return int(mism.sum()), int(both.sum())
+
+
+@pytest.fixture(scope="module")
+def soup():
+    desc = scenes.soup_scene(20000, seed=11)
+    gpu = nb.SceneBuffers.from_desc(desc, dedup=True)
+    orc = O.OracleScene(desc.vertices, desc.indices, desc.primitives(), dedup=True)
+    return desc, gpu, orc
+
+
+@pytest.mark.parametrize("kind", ["coherent", "incoherent"])
+def test_soup_closest_hit_matches_oracle(soup, kind):
+    desc, gpu, orc = soup
+    rays = scenes.coherent_rays(128, 96) if kind == "coherent" else scenes.incoherent_rays(20000, seed=5)
+    hits, inst = gpu.trace_host(rays)
+    rf, ru, cnt = orc.trace(rays)
+    assert cnt[:, 3].max() == 0
+    ties, both = compare_hits(hits, inst, gpu.export()["indices"], rf, ru)
+    assert both > 1000
+
+
+def test_soup_any_hit_agrees_on_occlusion(soup):
+    desc, gpu, orc = soup
+    rays = scenes.incoherent_rays(20000, seed=6)
+    any_hits, _ = gpu.trace_host(rays, any_hit=True)
+    closest, _ = gpu.trace_host(rays)
+    rf, _, _ = orc.trace(rays, any_hit=True)
+    g_occ = any_hits[:, 0] != NO_HIT
+    assert np.array_equal(g_occ, closest[:, 0] != NO_HIT)
+    assert np.array_equal(g_occ, rf[:, 0] != NO_HIT)
+    # an any-hit answer is a real hit: never closer than the closest one
+    assert np.all(any_hits[g_occ, 0] >= closest[g_occ, 0])
+
+
+def test_instanced_scene_primary_rays_match(tmp_path):
+    desc = scenes.spheres_scene(width=96, height=96)
+    sob = nb.sobol_burley_table()
+    for dedup in (True, False):
+        gpu = nb.SceneBuffers.from_desc(desc, dedup=dedup)
+        orc = O.OracleScene(desc.vertices, desc.indices, desc.primitives(), dedup=dedup)
+        rays = O.primary_rays(desc.clip_to_world, desc.width, desc.height, sob, 1)
+        hits, inst = gpu.trace_host(rays)
+        rf, ru, _ = orc.trace(rays)
+        compare_hits(hits, inst, gpu.export()["indices"], rf, ru)
+
+
+def test_scene_from_reference_buffers_traces_identically():
+    desc = scenes.spheres_scene(width=64, height=64)
+    orc = O.OracleScene(desc.vertices, desc.indices, desc.primitives(), dedup=False)
+    gpu = nb.SceneBuffers.from_bvh(orc.blas, orc.tlas, orc.instances, orc.vertices, orc.indices)
+    rays = scenes.incoherent_rays(8000, seed=9) * np.array([12, 12, 12, 0, 1, 1, 1, 0], np.float32)
+    hits, inst = gpu.trace_host(rays)
+    rf, ru, _ = orc.trace(rays)
+    compare_hits(hits, inst, orc.indices, rf, ru)
+
+
+def test_empty_query_and_miss_everything(soup):
+    desc, gpu, orc = soup
+    hits, inst = gpu.trace_host(np.zeros((0, 8), np.float32))
+    assert hits.shape == (0, 4)
+    away = np.zeros((64, 8), np.float32)
+    away[:, :3] = [5.0, 5.0, 5.0]
+    away[:, 4:7] = [1.0, 0.0, 0.0]
+    hits, inst = gpu.trace_host(away)
+    assert np.all(hits[:, 0] == NO_HIT) and np.all(inst == 0xFFFFFFFF)
