@@ -46,6 +46,9 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=12.0, help="CPU work per baseline sample")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--spp", type=int, default=64)
+    p.add_argument("--width", type=int, default=1920, help="smaller frames for profiling runs only")
+    p.add_argument("--height", type=int, default=1080)
+    p.add_argument("--batch-paths", type=int, default=0, help="paths per wavefront batch (0: library default)")
     return p.parse_args()
 
 
@@ -110,10 +113,9 @@ def measured_peaks():
         return 6800.0, "fallback"
 
 
-def build_workload(spp):
+def build_workload(args):
     from nbounce_gb300 import scenes
-    desc = scenes.instanced_scene(spp=spp)
-    return desc
+    return scenes.instanced_scene(spp=args.spp, width=args.width, height=args.height)
 
 
 def cpu_baseline(desc, sobol, seconds, threads):
@@ -153,13 +155,15 @@ def run_ours(args):
         torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
     dev = torch.device("cuda", local)
-    desc = build_workload(args.spp)
+    desc = build_workload(args)
     t0 = time.perf_counter()
     scene = nb.SceneBuffers.from_desc(desc, dedup=True)
     build_s = time.perf_counter() - t0
     env = nb.EnvMap(texels=desc.env_texels)
     cam = nb.camera_struct(desc.world_to_clip, desc.clip_to_world)
     pt = nb.Pathtracer(desc.width, desc.height, nb.Globals(bounces=desc.bounces))
+    if args.batch_paths:
+        pt.set_batch_paths(args.batch_paths)
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
 
@@ -261,7 +265,7 @@ def run_reference(args):
     if rank != 0:
         return None
     import nbounce_gb300 as nb
-    desc = build_workload(args.spp)
+    desc = build_workload(args)
     sobol = nb.sobol_burley_table()
     threads = os.cpu_count() or 1
     base, per_ray, osc = cpu_baseline(desc, sobol, min(args.cpu_seconds, 10.0), threads)

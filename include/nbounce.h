@@ -206,6 +206,11 @@ int nb_pathtracer_dispatch(nb_pathtracer* pt, const nb_scene* scene, const nb_ca
 int nb_pathtracer_render(nb_pathtracer* pt, const nb_scene* scene, const nb_camera* camera, const nb_env* env,
                          uint32_t n_samples, void* stream);
 
+/* Paths in flight per wavefront batch (default 2^25).  Work buffers take ~132 bytes per
+ * path; more paths keep late bounces busier.  No counterpart in the reference (it traces one
+ * sample per pixel per dispatch). */
+int nb_pathtracer_set_batch_paths(nb_pathtracer* pt, uint32_t paths);
+
 int nb_pathtracer_invalidate(nb_pathtracer* pt);                           /* pathtracer.rs:221-223 */
 int nb_pathtracer_resize(nb_pathtracer* pt, uint32_t width, uint32_t height); /* pathtracer.rs:208-210 */
 int nb_pathtracer_get_globals(const nb_pathtracer* pt, nb_globals* out);

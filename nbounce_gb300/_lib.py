@@ -106,6 +106,7 @@ def lib():
         "nb_pathtracer_output": ([vp, vp, vp, vp], i32),
         "nb_pathtracer_download": ([vp, vp, vp], i32),
         "nb_pathtracer_last_stats": ([vp, vp, vp, vp], i32),
+        "nb_pathtracer_set_batch_paths": ([vp, u32], i32),
         "nb_pathtracer_enable_timing": ([vp, i32], i32),
         "nb_pathtracer_kernel_times": ([vp, vp, i32, vp], i32),
         "nb_trace_rays": ([vp, vp, sz, u32, vp, vp, vp], i32),

@@ -116,6 +116,7 @@ struct nb_pathtracer {
   unsigned long long* d_rays = nullptr;
   PathBatch pb{};
   uint32_t capacity = 0;  // paths the work buffers hold
+  uint32_t batch_paths = 1u << 25;
   int sms = 1;
   // optional per-kernel event timing: (kind, start, stop) of every recorded launch
   bool timing = false;
@@ -487,8 +488,7 @@ static int ensure_capacity(nb_pathtracer* pt, uint32_t paths) {
 // samples per batch: enough paths in flight to fill the GPU, bounded memory
 static uint32_t batch_samples(const nb_pathtracer* pt, uint32_t remaining) {
   const uint64_t npix = (uint64_t)pt->width * pt->height;
-  const uint64_t target = 1ull << 23;  // ~8M paths per wave
-  uint64_t s = std::max<uint64_t>(1, target / std::max<uint64_t>(1, npix));
+  uint64_t s = std::max<uint64_t>(1, pt->batch_paths / std::max<uint64_t>(1, npix));
   return (uint32_t)std::min<uint64_t>(s, remaining);
 }
 
@@ -549,6 +549,12 @@ int nb_pathtracer_dispatch(nb_pathtracer* pt, const nb_scene* scene, const nb_ca
 int nb_pathtracer_render(nb_pathtracer* pt, const nb_scene* scene, const nb_camera* camera, const nb_env* env,
                          uint32_t n_samples, void* stream) {
   return render_samples(pt, scene, camera, env, n_samples, stream);
+}
+
+int nb_pathtracer_set_batch_paths(nb_pathtracer* pt, uint32_t paths) {
+  if (!pt || paths == 0 || paths > 0x7FFFFFFFu) return fail(NB_ERR_INVALID_ARG, "invalid batch size");
+  pt->batch_paths = paths;
+  return NB_OK;
 }
 
 int nb_pathtracer_enable_timing(nb_pathtracer* pt, int enable) {

@@ -51,169 +51,199 @@ struct Hit {
   uint32_t tri, inst;
 };
 
-struct TraceCounters {
-  uint32_t nodes, tris, insts;
+// Traversal state of one lane (one ray) in the persistent kernels.  The stack lives in
+// local memory; everything else stays in registers.
+struct Lane {
+  V3 wo, wd, winv;  // world ray
+  V3 ro, rd, rinv;  // ray of the current level (world, or instance-local inside a BLAS)
+  Hit h;
+  int sp, blas_base;
+  uint32_t inst_cur, inst_end, cur_inst;
+  uint32_t ray, iter;
+  bool in_blas;
 };
 
-// Closest (or any) hit of one world-space ray.  Returns the status bits it raised.
-template <bool kAny, bool kStats>
-__device__ uint32_t trace_ray(const DevScene& s, V3 wo, V3 wd, Hit* out, TraceCounters* cnt) {
-  Hit h;
-  h.t = kNoHit;
-  h.u = h.v = 0.0f;
-  h.tri = 0xFFFFFFFFu;
-  h.inst = 0xFFFFFFFFu;
-  uint32_t status = 0;
-  if (!s.has_tlas) {
-    *out = h;
-    return 0;
+__device__ __forceinline__ void push(Lane& L, uint2* stack, uint32_t ref, float d, uint32_t& status) {
+  if (L.sp < kStackSize) {
+    stack[L.sp] = make_uint2(ref, __float_as_uint(d));
+    ++L.sp;
+  } else {
+    status |= kStatusStackOverflow;
   }
-  const V3 winv = rcp3(wd);
-  V3 ro = wo, rd = wd, rinv = winv;
-  uint2 stack[kStackSize];
-  int sp = 0;
-  bool in_blas = false;
-  uint32_t inst_cur = 0, inst_end = 0, cur_inst = 0;
-  int blas_base = 0;
+}
 
-  auto push = [&](uint32_t ref, float d) {
-    if (sp < kStackSize) {
-      stack[sp] = make_uint2(ref, __float_as_uint(d));
-      ++sp;
-    } else {
-      status |= kStatusStackOverflow;
-    }
-  };
-  // enter the BLAS of instance j: transform the world ray (raytracing_sw.wgsl:202-206)
-  auto start_instance = [&](uint32_t j) {
-    const float4* it = s.inst_trace + 4 * (size_t)j;
-    float4 r0 = ld4(it), r1 = ld4(it + 1), r2 = ld4(it + 2);
-    uint32_t root = __float_as_uint(ld4(it + 3).x);
-    ro = V3{r0.x * wo.x + r0.y * wo.y + r0.z * wo.z + r0.w * 1.0f,
-            r1.x * wo.x + r1.y * wo.y + r1.z * wo.z + r1.w * 1.0f,
+// Enter the BLAS of instance j: transform the world ray (raytracing_sw.wgsl:202-206), test
+// the BLAS root box and push the root (raytracing_sw.wgsl:259-265).
+__device__ __forceinline__ void enter_instance(const DevScene& s, Lane& L, uint2* stack, uint32_t j,
+                                               uint32_t& status) {
+  const float4* it = s.inst_trace + 4 * (size_t)j;
+  const float4 r0 = ld4(it), r1 = ld4(it + 1), r2 = ld4(it + 2);
+  const uint32_t root = __float_as_uint(ld4(it + 3).x);
+  const V3 wo = L.wo, wd = L.wd;
+  L.ro = V3{r0.x * wo.x + r0.y * wo.y + r0.z * wo.z + r0.w * 1.0f, r1.x * wo.x + r1.y * wo.y + r1.z * wo.z + r1.w * 1.0f,
             r2.x * wo.x + r2.y * wo.y + r2.z * wo.z + r2.w * 1.0f};
-    rd = V3{r0.x * wd.x + r0.y * wd.y + r0.z * wd.z, r1.x * wd.x + r1.y * wd.y + r1.z * wd.z,
+  L.rd = V3{r0.x * wd.x + r0.y * wd.y + r0.z * wd.z, r1.x * wd.x + r1.y * wd.y + r1.z * wd.z,
             r2.x * wd.x + r2.y * wd.y + r2.z * wd.z};
-    rinv = rcp3(rd);
-    cur_inst = j;
-    float4 lo = ld4(s.blas_roots + 2 * (size_t)root), hi = ld4(s.blas_roots + 2 * (size_t)root + 1);
-    float d = slab(ro, rinv, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
-    if (kStats) { cnt->nodes += 1; cnt->insts += 1; }
-    if (d < h.t) push(__float_as_uint(lo.w), d);
-  };
+  L.rinv = rcp3(L.rd);
+  L.cur_inst = j;
+  const float4 lo = ld4(s.blas_roots + 2 * (size_t)root), hi = ld4(s.blas_roots + 2 * (size_t)root + 1);
+  const float d = slab(L.ro, L.rinv, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
+  if (d < L.h.t) push(L, stack, __float_as_uint(lo.w), d, status);
+}
 
-  {
-    float4 lo = s.tlas_root_lo, hi = s.tlas_root_hi;
-    float d = slab(wo, winv, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
-    if (kStats) cnt->nodes += 1;
-    if (d < h.t) push(__float_as_uint(lo.w), d);
+// Start a new ray: test the TLAS root and push it (raytracing_sw.wgsl:182-191).
+__device__ __forceinline__ void lane_start(const DevScene& s, Lane& L, uint2* stack, V3 o, V3 d, uint32_t& status) {
+  L.wo = o; L.wd = d; L.winv = rcp3(d);
+  L.ro = o; L.rd = d; L.rinv = L.winv;
+  L.h.t = kNoHit; L.h.u = 0.0f; L.h.v = 0.0f; L.h.tri = 0xFFFFFFFFu; L.h.inst = 0xFFFFFFFFu;
+  L.sp = 0; L.blas_base = 0; L.in_blas = false; L.iter = 0;
+  L.inst_cur = L.inst_end = L.cur_inst = 0;
+  if (!s.has_tlas) return;
+  const float4 lo = s.tlas_root_lo, hi = s.tlas_root_hi;
+  const float dr = slab(o, L.winv, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
+  if (dr < L.h.t) push(L, stack, __float_as_uint(lo.w), dr, status);
+}
+
+// One stack pop of the two-level traversal.  Returns true when the ray is finished.
+template <bool kAny>
+__device__ __forceinline__ bool lane_step(const DevScene& s, Lane& L, uint2* stack, uint32_t& status) {
+  if (++L.iter > kIterationCap) {
+    status |= kStatusIterationCap;
+    return true;
   }
-  uint32_t iter = 0;
-  while (true) {
-    if (++iter > kIterationCap) {
-      status |= kStatusIterationCap;
-      break;
+  if (L.in_blas && L.sp == L.blas_base) {
+    if (L.inst_cur < L.inst_end) {  // next instance of the TLAS leaf (raytracing_sw.wgsl:201)
+      enter_instance(s, L, stack, L.inst_cur++, status);
+      return false;
     }
-    if (in_blas && sp == blas_base) {
-      if (inst_cur < inst_end) {
-        start_instance(inst_cur++);
-        continue;
+    L.in_blas = false;
+    L.ro = L.wo; L.rd = L.wd; L.rinv = L.winv;
+  }
+  if (L.sp == 0) return true;
+  --L.sp;
+  const uint2 e = stack[L.sp];
+  if (__uint_as_float(e.y) >= L.h.t) return false;  // raytracing_sw.wgsl:197,271
+  const uint32_t ref = e.x;
+  if (ref & kLeafBit) {
+    const uint32_t first = ref & ~kLeafBit;
+    if (!L.in_blas) {
+      // TLAS leaf: its instances one after the other (raytracing_sw.wgsl:200-217)
+      const uint32_t n = __float_as_uint(ld4(s.inst_trace + 4 * (size_t)first + 3).y);
+      L.inst_cur = first + 1;
+      L.inst_end = first + n;
+      L.in_blas = true;
+      L.blas_base = L.sp;
+      enter_instance(s, L, stack, first, status);
+      return false;
+    }
+    // BLAS leaf: Moller-Trumbore over the leaf's triangles (raytracing_sw.wgsl:51-78, 274-286)
+    const float4* tp = s.tris + 3 * (size_t)first;
+    float4 a = ld4(tp);
+    const uint32_t n = __float_as_uint(a.w);
+    for (uint32_t k = 0; k < n; ++k) {
+      if (k) a = ld4(tp + 3 * k);
+      const float4 b = ld4(tp + 3 * k + 1), c = ld4(tp + 3 * k + 2);
+      const V3 e1 = xyz(b), e2 = xyz(c);
+      const V3 hv = cross(L.rd, e2);
+      const float det = dot(e1, hv);
+      if (det < kEps) continue;
+      const float inv_det = 1.0f / det;
+      const V3 sv = L.ro - xyz(a);
+      const float u = inv_det * dot(sv, hv);
+      if (u < 0.0f || u > 1.0f) continue;
+      const V3 q = cross(sv, e1);
+      const float v = inv_det * dot(L.rd, q);
+      if (v < 0.0f || u + v > 1.0f) continue;
+      const float t = inv_det * dot(e2, q);
+      if (t < kBias) continue;
+      if (t < L.h.t) {
+        L.h.t = t; L.h.u = u; L.h.v = v;
+        L.h.tri = first + k;
+        L.h.inst = L.cur_inst;
+        if (kAny) return true;
       }
-      in_blas = false;
-      ro = wo; rd = wd; rinv = winv;
     }
-    if (sp == 0) break;
-    --sp;
-    uint2 e = stack[sp];
-    if (__uint_as_float(e.y) >= h.t) continue;
-    const uint32_t ref = e.x;
-    if (ref & kLeafBit) {
-      const uint32_t first = ref & ~kLeafBit;
-      if (!in_blas) {
-        // TLAS leaf: instances [first, first + n) one after the other (raytracing_sw.wgsl:200-217)
-        uint32_t n = __float_as_uint(ld4(s.inst_trace + 4 * (size_t)first + 3).y);
-        inst_cur = first;
-        inst_end = first + n;
-        in_blas = true;
-        blas_base = sp;
-        start_instance(inst_cur++);
-      } else {
-        // BLAS leaf: Moller-Trumbore over the leaf's triangles (raytracing_sw.wgsl:274-286)
-        const float4* tp = s.tris + 3 * (size_t)first;
-        float4 a = ld4(tp);
-        const uint32_t n = __float_as_uint(a.w);
-        for (uint32_t k = 0; k < n; ++k) {
-          if (k) a = ld4(tp + 3 * k);
-          float4 b = ld4(tp + 3 * k + 1), c = ld4(tp + 3 * k + 2);
-          if (kStats) cnt->tris += 1;
-          V3 e1 = xyz(b), e2 = xyz(c);
-          V3 hv = cross(rd, e2);
-          float det = dot(e1, hv);
-          if (det < kEps) continue;
-          float inv_det = 1.0f / det;
-          V3 sv = ro - xyz(a);
-          float u = inv_det * dot(sv, hv);
-          if (u < 0.0f || u > 1.0f) continue;
-          V3 q = cross(sv, e1);
-          float v = inv_det * dot(rd, q);
-          if (v < 0.0f || u + v > 1.0f) continue;
-          float t = inv_det * dot(e2, q);
-          if (t < kBias) continue;
-          if (t < h.t) {
-            h.t = t; h.u = u; h.v = v;
-            h.tri = first + k;
-            h.inst = cur_inst;
-            if (kAny) {
-              *out = h;
-              return status;
-            }
-          }
+    return false;
+  }
+  // inner node: test both children, push far then near (raytracing_sw.wgsl:218-247)
+  const float4* np = (L.in_blas ? s.blas_nodes : s.tlas_nodes) + 4 * (size_t)ref;
+  const float4 q0 = ld4(np), q1 = ld4(np + 1), q2 = ld4(np + 2), q3 = ld4(np + 3);
+  const float dl = slab(L.ro, L.rinv, q0.x, q0.y, q0.z, q0.w, q2.x, q2.y);
+  const float dr = slab(L.ro, L.rinv, q1.x, q1.y, q1.z, q1.w, q2.z, q2.w);
+  const uint32_t lref = __float_as_uint(q3.x), rref = __float_as_uint(q3.y);
+  uint32_t fref = lref, nref = rref;
+  float fd = dl, nd = dr;
+  if (dl < dr) { fref = rref; fd = dr; nref = lref; nd = dl; }
+  if (fd < L.h.t) push(L, stack, fref, fd, status);
+  if (nd < L.h.t) push(L, stack, nref, nd, status);
+  return false;
+}
+
+// Persistent traversal over rays [0, n): every lane whose ray finished takes the next ray
+// (one warp-aggregated atomic per refill), so warps stay full until the work runs out
+// instead of waiting for their slowest ray.
+constexpr uint32_t kFullMask = 0xFFFFFFFFu;
+template <bool kAny, class Io>
+__device__ __forceinline__ void trace_persistent(const DevScene& s, const Io& io, uint32_t n, uint32_t* fetch,
+                                                 uint32_t* status_out) {
+  const uint32_t lane = threadIdx.x & 31;
+  const uint32_t lt_mask = (1u << lane) - 1u;
+  uint2 stack[kStackSize];
+  Lane L;
+  bool active = false, retired = false;
+  uint32_t status = 0;
+  while (true) {
+    const bool want = !active && !retired;
+    const uint32_t wmask = __ballot_sync(kFullMask, want);
+    if (wmask) {
+      const int leader = __ffs(wmask) - 1;
+      uint32_t base = 0;
+      if ((int)lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(wmask));
+      base = __shfl_sync(kFullMask, base, leader);
+      if (want) {
+        const uint32_t idx = base + (uint32_t)__popc(wmask & lt_mask);
+        if (idx < n) {
+          V3 o, d;
+          io.load(idx, o, d);
+          L.ray = idx;
+          lane_start(s, L, stack, o, d, status);
+          active = true;
+        } else {
+          retired = true;
         }
       }
-    } else {
-      // inner node: test both children, push far then near (raytracing_sw.wgsl:218-247)
-      const float4* np = (in_blas ? s.blas_nodes : s.tlas_nodes) + 4 * (size_t)ref;
-      float4 q0 = ld4(np), q1 = ld4(np + 1), q2 = ld4(np + 2), q3 = ld4(np + 3);
-      float dl = slab(ro, rinv, q0.x, q0.y, q0.z, q0.w, q2.x, q2.y);
-      float dr = slab(ro, rinv, q1.x, q1.y, q1.z, q1.w, q2.z, q2.w);
-      if (kStats) cnt->nodes += 2;
-      uint32_t lref = __float_as_uint(q3.x), rref = __float_as_uint(q3.y);
-      uint32_t fref = lref, nref = rref;
-      float fd = dl, nd = dr;
-      if (dl < dr) { fref = rref; fd = dr; nref = lref; nd = dl; }
-      if (fd < h.t) push(fref, fd);
-      if (nd < h.t) push(nref, nd);
+    }
+    if (!__any_sync(kFullMask, active)) break;
+    if (active && lane_step<kAny>(s, L, stack, status)) {
+      io.store(L.ray, L.h);
+      active = false;
     }
   }
-  *out = h;
-  return status;
+  if (status) atomicOr(status_out, status);
 }
+
+struct QueryIo {  // caller rays of 8 floats (origin, pad, direction, pad)
+  const float4* rays;
+  float4* hits;
+  uint32_t* inst;
+  __device__ __forceinline__ void load(uint32_t i, V3& o, V3& d) const {
+    o = xyz(__ldg(rays + 2 * (size_t)i));
+    d = xyz(__ldg(rays + 2 * (size_t)i + 1));
+  }
+  __device__ __forceinline__ void store(uint32_t i, const Hit& h) const {
+    hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
+    if (inst) inst[i] = h.inst;
+  }
+};
 
 // ------------------------------------------------------------------------------------------
 // traversal-only query (nb_trace_rays)
 // ------------------------------------------------------------------------------------------
 template <bool kAny>
-__global__ void __launch_bounds__(128) k_trace_rays(DevScene s, const float4* __restrict__ rays, uint32_t n,
+__global__ void __launch_bounds__(128, 8) k_trace_rays(DevScene s, const float4* __restrict__ rays, uint32_t n,
                                                      float4* __restrict__ hits, uint32_t* __restrict__ inst,
                                                      uint32_t* __restrict__ fetch, uint32_t* __restrict__ status) {
-  const int lane = threadIdx.x & 31;
-  uint32_t st = 0;
-  while (true) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(fetch, 32u);
-    base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    if (base >= n) break;
-    uint32_t i = base + lane;
-    if (i < n) {
-      float4 o = __ldg(rays + 2 * (size_t)i), d = __ldg(rays + 2 * (size_t)i + 1);
-      Hit h;
-      TraceCounters c;
-      st |= trace_ray<kAny, false>(s, xyz(o), xyz(d), &h, &c);
-      hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
-      if (inst) inst[i] = h.inst;
-    }
-  }
-  if (st) atomicOr(status, st);
+  trace_persistent<kAny>(s, QueryIo{rays, hits, inst}, n, fetch, status);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -260,55 +290,70 @@ __global__ void __launch_bounds__(256) k_raygen(PathBatch pb, CameraParams cam) 
   }
 }
 
-__global__ void __launch_bounds__(128) k_trace_wave(DevScene s, PathBatch pb, uint32_t bounce,
+struct WaveIo {  // the bounce's ray queue and hit buffers
+  const float4* qo;
+  const float4* qd;
+  float4* hits;
+  uint32_t* inst;
+  __device__ __forceinline__ void load(uint32_t i, V3& o, V3& d) const {
+    o = xyz(qo[i]);
+    d = xyz(qd[i]);
+  }
+  __device__ __forceinline__ void store(uint32_t i, const Hit& h) const {
+    hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
+    inst[i] = h.inst;
+  }
+};
+
+__global__ void __launch_bounds__(128, 8) k_trace_wave(DevScene s, PathBatch pb, uint32_t bounce,
                                                     unsigned long long* __restrict__ ray_total) {
   const uint32_t n = pb.counts[bounce];
-  const float4* __restrict__ qo = (bounce & 1) ? pb.q_o[1] : pb.q_o[0];
-  const float4* __restrict__ qd = (bounce & 1) ? pb.q_d[1] : pb.q_d[0];
-  const int lane = threadIdx.x & 31;
-  uint32_t st = 0;
-  while (true) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(pb.fetch + bounce, 32u);
-    base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    if (base >= n) break;
-    uint32_t i = base + lane;
-    if (i < n) {
-      float4 o = qo[i], d = qd[i];
-      Hit h;
-      TraceCounters c;
-      st |= trace_ray<false, false>(s, xyz(o), xyz(d), &h, &c);
-      pb.hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
-      pb.hit_inst[i] = h.inst;
-    }
-  }
-  if (st) atomicOr(pb.status, st);
+  const WaveIo io{(bounce & 1) ? pb.q_o[1] : pb.q_o[0], (bounce & 1) ? pb.q_d[1] : pb.q_d[0], pb.hits, pb.hit_inst};
+  trace_persistent<false>(s, io, n, pb.fetch + bounce, pb.status);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(ray_total, (unsigned long long)n);
 }
 
-// equirect lookup, evaluated in binary64 (the oracle's definition): u = atan2(x, -z)/(2 pi) + 0.5,
-// v = acos(y)/pi of the normalised direction, bilinear with wrap in u and clamp in v
+// atan2 / acos in binary32 by octant reduction and a degree-7 polynomial in x^2 for atan on
+// [0,1] (fitted for this build, max error 1.7e-7), Horner without fusion: the oracle
+// evaluates the identical sequence, so both sides agree bit for bit.
+__device__ __forceinline__ float nb_atan2(float y, float x) {
+  const float P[8] = {0x1.fffffcp-1f, -0x1.5551dp-2f, 0x1.98faep-3f, -0x1.1f1e82p-3f,
+                      0x1.96172p-4f,  -0x1.e75096p-5f, 0x1.8d5abp-6f, -0x1.3394dap-8f};
+  float ax = fabsf(x), ay = fabsf(y);
+  float mx = ax > ay ? ax : ay, mn = ax > ay ? ay : ax;
+  float a = mx > 0.0f ? mn / mx : 0.0f;
+  float a2 = a * a;
+  float p = P[7];
+#pragma unroll
+  for (int k = 6; k >= 0; --k) p = p * a2 + P[k];
+  float r = a * p;
+  if (ay > ax) r = 1.57079637f - r;
+  if (x < 0.0f) r = 3.14159274f - r;
+  if (y < 0.0f) r = -r;
+  return r;
+}
+__device__ __forceinline__ float nb_acos(float y) { return nb_atan2(sqrtf((1.0f - y) * (1.0f + y)), y); }
+
+// equirect lookup (the oracle's definition): u = atan2(d.x, -d.z)/(2 pi) + 0.5, v = acos(d.y)/pi
+// of the normalised direction, bilinear with wrap in u and clamp in v; NaN directions see black
 __device__ V3 env_lookup(const DevEnv& env, V3 dir) {
   if (env.kind == kEnvConstant) return V3{env.r, env.g, env.b};
-  double dx = dir.x, dy = dir.y, dz = dir.z;
-  double l = sqrt(dx * dx + dy * dy + dz * dz);
-  dx /= l; dy /= l; dz /= l;
-  const double kPiD = 3.14159265358979323846;
-  double u = atan2(dx, -dz) / (2.0 * kPiD) + 0.5;
-  double v = acos(fmax(-1.0, fmin(1.0, dy))) / kPiD;
-  double fx = u * env.width - 0.5, fy = v * env.height - 0.5;
-  double x0 = floor(fx), y0 = floor(fy);
-  double tx = fx - x0, ty = fy - y0;
-  long W = env.width, H = env.height;
-  long xi0 = (((long)x0 % W) + W) % W, xi1 = (((long)x0 + 1) % W + W) % W;
-  long yi0 = (long)y0 < 0 ? 0 : ((long)y0 > H - 1 ? H - 1 : (long)y0);
-  long yi1 = (long)y0 + 1 < 0 ? 0 : ((long)y0 + 1 > H - 1 ? H - 1 : (long)y0 + 1);
-  float4 t00 = __ldg(env.texels + yi0 * W + xi0), t10 = __ldg(env.texels + yi0 * W + xi1);
-  float4 t01 = __ldg(env.texels + yi1 * W + xi0), t11 = __ldg(env.texels + yi1 * W + xi1);
-  double c0 = ((double)t00.x * (1 - tx) + (double)t10.x * tx) * (1 - ty) + ((double)t01.x * (1 - tx) + (double)t11.x * tx) * ty;
-  double c1 = ((double)t00.y * (1 - tx) + (double)t10.y * tx) * (1 - ty) + ((double)t01.y * (1 - tx) + (double)t11.y * tx) * ty;
-  double c2 = ((double)t00.z * (1 - tx) + (double)t10.z * tx) * (1 - ty) + ((double)t01.z * (1 - tx) + (double)t11.z * tx) * ty;
-  return V3{(float)c0, (float)c1, (float)c2};
+  V3 d = normalize(dir);
+  float u = nb_atan2(d.x, -d.z) * 0.159154943f + 0.5f;
+  float v = nb_acos(fminf(fmaxf(d.y, -1.0f), 1.0f)) * 0.318309886f;
+  float fx = u * (float)env.width - 0.5f, fy = v * (float)env.height - 0.5f;
+  if (fx != fx || fy != fy) return V3{0.0f, 0.0f, 0.0f};
+  float x0 = floorf(fx), y0 = floorf(fy);
+  float tx = fx - x0, ty = fy - y0;
+  int W = (int)env.width, H = (int)env.height;
+  int xi = (int)x0, yi = (int)y0;
+  int xa = ((xi % W) + W) % W, xb = (((xi + 1) % W) + W) % W;
+  int ya = yi < 0 ? 0 : (yi > H - 1 ? H - 1 : yi), yb = yi + 1 < 0 ? 0 : (yi + 1 > H - 1 ? H - 1 : yi + 1);
+  float4 t00 = __ldg(env.texels + (size_t)ya * W + xa), t10 = __ldg(env.texels + (size_t)ya * W + xb);
+  float4 t01 = __ldg(env.texels + (size_t)yb * W + xa), t11 = __ldg(env.texels + (size_t)yb * W + xb);
+  return V3{(t00.x * (1.0f - tx) + t10.x * tx) * (1.0f - ty) + (t01.x * (1.0f - tx) + t11.x * tx) * ty,
+            (t00.y * (1.0f - tx) + t10.y * tx) * (1.0f - ty) + (t01.y * (1.0f - tx) + t11.y * tx) * ty,
+            (t00.z * (1.0f - tx) + t10.z * tx) * (1.0f - ty) + (t01.z * (1.0f - tx) + t11.z * tx) * ty};
 }
 
 // sample_vndf_iso (pathtracing.wgsl:68-98)

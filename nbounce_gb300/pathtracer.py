@@ -256,6 +256,9 @@ class Pathtracer:
         check(lib().nb_pathtracer_last_stats(self._h, C.byref(rays), C.byref(st), _stream(stream)))
         return int(rays.value), int(st.value)
 
+    def set_batch_paths(self, paths):
+        check(lib().nb_pathtracer_set_batch_paths(self._h, int(paths)))
+
     def enable_timing(self, enable=True):
         check(lib().nb_pathtracer_enable_timing(self._h, int(enable)))
 

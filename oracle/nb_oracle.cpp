@@ -40,6 +40,7 @@
 #include <limits>
 #include <map>
 #include <thread>
+#include <type_traits>
 #include <vector>
 
 #include "joe_kuo_68.inc"
@@ -864,10 +865,54 @@ static V3<R> sample_rendering_eq(const RenderArgs& a, uint32_t sample, const flo
   return {R(0), R(0), R(0)};
 }
 
-// equirect lookup: u = atan2(d.x, -d.z) / (2 pi) + 0.5, v = acos(d.y) / pi on the normalized
-// direction, bilinear with wrap in u and clamp in v.  Evaluated in binary64 and rounded.
+// Equirect lookup (the build's definition; the reference samples a cube map): on the
+// normalised direction d, u = atan2(d.x, -d.z) / (2 pi) + 0.5 and v = acos(d.y) / pi; bilinear
+// filtering with wrap in u and clamp in v, texel centres at (i + 0.5) / size; a NaN direction
+// sees black.  binary32: atan on [0,1] is x * P(x^2) with a degree-7 P fitted for this build
+// (max error 1.7e-7), atan2/acos by octant reduction, Horner without fusion.  binary64 (truth
+// mode): libm atan2/acos.
+constexpr float kAtanP[8] = {0x1.fffffcp-1f, -0x1.5551dp-2f, 0x1.98faep-3f, -0x1.1f1e82p-3f,
+                             0x1.96172p-4f,  -0x1.e75096p-5f, 0x1.8d5abp-6f, -0x1.3394dap-8f};
+static inline float atan2_f32(float y, float x) {
+  float ax = std::fabs(x), ay = std::fabs(y);
+  float mx = ax > ay ? ax : ay, mn = ax > ay ? ay : ax;
+  float a = mx > 0.0f ? mn / mx : 0.0f;
+  float a2 = a * a;
+  float p = kAtanP[7];
+  for (int k = 6; k >= 0; --k) p = p * a2 + kAtanP[k];
+  float r = a * p;
+  if (ay > ax) r = 1.57079637f - r;
+  if (x < 0.0f) r = 3.14159274f - r;
+  if (y < 0.0f) r = -r;
+  return r;
+}
+static inline float acos_f32(float y) { return atan2_f32(std::sqrt((1.0f - y) * (1.0f + y)), y); }
+
+static V3<float> env_lookup_f32(const or_env& env, V3<float> dir) {
+  V3<float> d = normalize(dir);
+  float u = atan2_f32(d.x, -d.z) * 0.159154943f + 0.5f;
+  float v = acos_f32(wmin(wmax(d.y, -1.0f), 1.0f)) * 0.318309886f;
+  float fx = u * (float)env.width - 0.5f, fy = v * (float)env.height - 0.5f;
+  if (fx != fx || fy != fy) return {0.0f, 0.0f, 0.0f};
+  float x0 = std::floor(fx), y0 = std::floor(fy);
+  float tx = fx - x0, ty = fy - y0;
+  int W = (int)env.width, H = (int)env.height;
+  int xi = (int)x0, yi = (int)y0;
+  int xa = ((xi % W) + W) % W, xb = (((xi + 1) % W) + W) % W;
+  int ya = yi < 0 ? 0 : (yi > H - 1 ? H - 1 : yi), yb = yi + 1 < 0 ? 0 : (yi + 1 > H - 1 ? H - 1 : yi + 1);
+  const float* t00 = env.texels + 4 * ((size_t)ya * W + xa);
+  const float* t10 = env.texels + 4 * ((size_t)ya * W + xb);
+  const float* t01 = env.texels + 4 * ((size_t)yb * W + xa);
+  const float* t11 = env.texels + 4 * ((size_t)yb * W + xb);
+  float c[3];
+  for (int ch = 0; ch < 3; ++ch)
+    c[ch] = (t00[ch] * (1.0f - tx) + t10[ch] * tx) * (1.0f - ty) + (t01[ch] * (1.0f - tx) + t11[ch] * tx) * ty;
+  return {c[0], c[1], c[2]};
+}
+
 template <class R> static V3<R> env_lookup(const or_env& env, V3<R> dir) {
   if (env.kind == 0) return {R(env.color[0]), R(env.color[1]), R(env.color[2])};
+  if constexpr (std::is_same<R, float>::value) return env_lookup_f32(env, dir);
   double dx = dir.x, dy = dir.y, dz = dir.z;
   double l = std::sqrt(dx * dx + dy * dy + dz * dz);
   dx /= l; dy /= l; dz /= l;
