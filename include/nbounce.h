@@ -118,7 +118,7 @@ typedef struct nb_pathtracer nb_pathtracer;
 typedef struct nb_scene_info {
   uint64_t n_vertices, n_triangles, n_instances, n_blas_roots;
   uint64_t n_blas_nodes_ref, n_tlas_nodes_ref;   /* reference-layout node counts */
-  uint64_t n_blas_nodes_gpu, n_tlas_nodes_gpu;   /* device node records (one per inner node) */
+  uint64_t n_blas_nodes_gpu, n_tlas_nodes_gpu;   /* device 8-wide node records */
   uint64_t device_bytes;
   double build_ms;                               /* host BVH build time */
 } nb_scene_info;
@@ -206,7 +206,7 @@ int nb_pathtracer_dispatch(nb_pathtracer* pt, const nb_scene* scene, const nb_ca
 int nb_pathtracer_render(nb_pathtracer* pt, const nb_scene* scene, const nb_camera* camera, const nb_env* env,
                          uint32_t n_samples, void* stream);
 
-/* Paths in flight per wavefront batch (default 2^25).  Work buffers take ~132 bytes per
+/* Paths in flight per wavefront batch (default 2^27).  Work buffers take ~132 bytes per
  * path; more paths keep late bounces busier.  No counterpart in the reference (it traces one
  * sample per pixel per dispatch). */
 int nb_pathtracer_set_batch_paths(nb_pathtracer* pt, uint32_t paths);

@@ -116,7 +116,7 @@ struct nb_pathtracer {
   unsigned long long* d_rays = nullptr;
   PathBatch pb{};
   uint32_t capacity = 0;  // paths the work buffers hold
-  uint32_t batch_paths = 1u << 25;
+  uint32_t batch_paths = 1u << 27;
   int sms = 1;
   // optional per-kernel event timing: (kind, start, stop) of every recorded launch
   bool timing = false;
@@ -152,34 +152,25 @@ static int upload_scene(nb_scene* s) {
   int st = to_device_layout(&h);
   if (st) return st;
   nbd::DevScene& d = s->dev;
-  const GpuNode *gb = nullptr, *gt = nullptr;
-  const GpuRoot* br = nullptr;
+  const WideNode *wb = nullptr, *wt = nullptr;
   const GpuInstTrace* it = nullptr;
   const GpuInstShade* is = nullptr;
   const GpuTri* tr = nullptr;
   const GpuVAttr* va = nullptr;
   const uint32_t* ti = nullptr;
-  if ((st = s->arena.upload(h.gblas, &gb)) || (st = s->arena.upload(h.gtlas, &gt)) ||
-      (st = s->arena.upload(h.blas_roots, &br)) || (st = s->arena.upload(h.itrace, &it)) ||
-      (st = s->arena.upload(h.ishade, &is)) || (st = s->arena.upload(h.tris, &tr)) ||
-      (st = s->arena.upload(h.vattr, &va)) || (st = s->arena.upload(h.indices, &ti)))
+  if ((st = s->arena.upload(h.wblas, &wb)) || (st = s->arena.upload(h.wtlas, &wt)) ||
+      (st = s->arena.upload(h.itrace, &it)) || (st = s->arena.upload(h.ishade, &is)) ||
+      (st = s->arena.upload(h.tris, &tr)) || (st = s->arena.upload(h.vattr, &va)) ||
+      (st = s->arena.upload(h.indices, &ti)))
     return st;
-  d.blas_nodes = (const float4*)gb;
-  d.tlas_nodes = (const float4*)gt;
-  d.blas_roots = (const float4*)br;
+  d.blas_wide = (const float4*)wb;
+  d.tlas_wide = (const float4*)wt;
   d.inst_trace = (const float4*)it;
   d.inst_shade = (const float4*)is;
   d.tris = (const float4*)tr;
   d.vattr = (const float4*)va;
   d.tri_idx = ti;
   d.has_tlas = h.has_tlas ? 1u : 0u;
-  float lo[4], hi[4];
-  std::memcpy(lo, h.tlas_root.mn, 12);
-  std::memcpy(&lo[3], &h.tlas_root.ref, 4);
-  std::memcpy(hi, h.tlas_root.mx, 12);
-  hi[3] = 0.0f;
-  d.tlas_root_lo = make_float4(lo[0], lo[1], lo[2], lo[3]);
-  d.tlas_root_hi = make_float4(hi[0], hi[1], hi[2], hi[3]);
   d.n_tris = (uint32_t)h.tris.size();
   d.n_inst = (uint32_t)h.itrace.size();
   d.n_vertices = (uint32_t)h.vertices.size();
@@ -189,8 +180,10 @@ static int upload_scene(nb_scene* s) {
   s->d_status = s->d_fetch + 1;
   NB_CUDA(cudaMemset(p, 0, 2 * sizeof(uint32_t)), "cudaMemset");
   // drop device-layout host copies; keep the reference-layout buffers for nb_scene_export
-  std::vector<GpuNode>().swap(h.gblas);
-  std::vector<GpuNode>().swap(h.gtlas);
+  h.wblas_nodes = h.wblas.size();
+  h.wtlas_nodes = h.wtlas.size();
+  std::vector<WideNode>().swap(h.wblas);
+  std::vector<WideNode>().swap(h.wtlas);
   std::vector<GpuTri>().swap(h.tris);
   std::vector<GpuVAttr>().swap(h.vattr);
   s->sms = sm_count();
@@ -324,14 +317,11 @@ int nb_scene_get_info(const nb_scene* s, nb_scene_info* info) {
   info->n_vertices = h.vertices.size();
   info->n_triangles = h.indices.size() / 3;
   info->n_instances = h.instances.size();
-  info->n_blas_roots = h.blas_roots.size();
+  info->n_blas_roots = h.wblas_root.size();
   info->n_blas_nodes_ref = h.blas.size();
   info->n_tlas_nodes_ref = h.tlas.size();
-  size_t inner_b = 0, inner_t = 0;
-  for (const auto& n : h.blas) inner_b += n.end == 0;
-  for (const auto& n : h.tlas) inner_t += n.end == 0;
-  info->n_blas_nodes_gpu = inner_b;
-  info->n_tlas_nodes_gpu = inner_t;
+  info->n_blas_nodes_gpu = s->uploaded ? h.wblas_nodes : h.wblas.size();
+  info->n_tlas_nodes_gpu = s->uploaded ? h.wtlas_nodes : h.wtlas.size();
   info->device_bytes = s->arena.bytes;
   info->build_ms = h.build_ms;
   return NB_OK;

@@ -97,16 +97,13 @@ __device__ __forceinline__ float fract(float x) { return x - floorf(x); }
 
 // Device view of a scene (pointers into library-owned device memory).
 struct DevScene {
-  const float4* tlas_nodes;   // 4 float4 per inner node
-  const float4* blas_nodes;   // 4 float4 per inner node
-  const float4* blas_roots;   // 2 float4 per BLAS root: (min.xyz, ref), (max.xyz, 0)
-  const float4* inst_trace;   // 4 float4 per instance
-  const float4* inst_shade;   // 6 float4 per instance
-  const float4* tris;         // 3 float4 per triangle
-  const uint32_t* tri_idx;    // 3 vertex ids per triangle
+  const float4* tlas_wide;    // 5 float4 per 8-wide TLAS node; the root is node 0
+  const float4* blas_wide;    // 5 float4 per 8-wide BLAS node
+  const float4* inst_trace;   // 4 float4 per instance, in wide-TLAS leaf order
+  const float4* inst_shade;   // 6 float4 per instance, reference (TLAS-permuted) order
+  const float4* tris;         // 3 float4 per triangle, in wide-BLAS leaf order
+  const uint32_t* tri_idx;    // 3 vertex ids per reference triangle
   const float4* vattr;        // 2 float4 per vertex
-  float4 tlas_root_lo;        // (min.xyz, ref bits)
-  float4 tlas_root_hi;        // (max.xyz, 0)
   uint32_t has_tlas;
   uint32_t n_tris, n_inst, n_vertices;
 };

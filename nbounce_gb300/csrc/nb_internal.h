@@ -6,15 +6,14 @@
 // two separate 32-byte nodes and every triangle through three indexed 48-byte vertex loads
 // (raytracing_sw.wgsl:218-225, 275-279).  The device layout keeps the same trees but packs
 // what one traversal step touches into 16-byte-aligned records read with 128-bit loads:
-//   GpuNode      64 B  both children's boxes + child references of one inner node
-//   GpuRoot      32 B  a tree's root box + reference (the traversal tests the root box first)
+//   WideNode     80 B  8 children of a collapsed node: 8-bit quantised boxes, slot metadata
 //   GpuTri       48 B  v0, e1 = v1 - v0, e2 = v2 - v0 (the subtractions intersect_triangle
-//                      performs), leaf length in v0.w of a leaf's first triangle
-//   GpuInstTrace 64 B  the three rows of world_to_local used to transform rays, BLAS root id,
-//                      TLAS leaf length in the first instance of each TLAS leaf
+//                      performs) + the reference triangle index
+//   GpuInstTrace 64 B  the three rows of world_to_local used to transform rays, BLAS root,
+//                      reference instance index
 //   GpuInstShade 96 B  what intersect_scene/shading read from an instance
 //   GpuVAttr     32 B  vertex normal + tangent (positions live in GpuTri)
-// A child reference is either an inner-node index or kLeafBit | first primitive.
+// Triangles and instances are stored in the order of the wide trees' leaves.
 #pragma once
 
 #include <cstdint>
@@ -30,31 +29,18 @@ constexpr uint32_t kLdsStride = 17u;      // pathtracing.wgsl:4 (fixed, independ
 constexpr uint32_t kLdsPerBounce = 2u;    // pathtracing.wgsl:2
 constexpr uint32_t kMaxSampleCount = 1024u;  // pathtracer.rs:56
 
-struct alignas(16) GpuNode {
-  float q0[4];    // c0.min.x, c0.max.x, c0.min.y, c0.max.y
-  float q1[4];    // c1.min.x, c1.max.x, c1.min.y, c1.max.y
-  float q2[4];    // c0.min.z, c0.max.z, c1.min.z, c1.max.z
-  uint32_t ref[2];
-  uint32_t pad[2];
-};
-struct alignas(16) GpuRoot {
-  float mn[3];
-  uint32_t ref;
-  float mx[3];
-  uint32_t pad;
-};
 struct alignas(16) GpuTri {
   float v0[3];
-  uint32_t leaf_count;
+  uint32_t pad0;
   float e1[3];
-  uint32_t pad1;
+  uint32_t ref_index;  // index in the reference's permuted triangle list (reported by hits)
   float e2[3];
   uint32_t pad2;
 };
 struct alignas(16) GpuInstTrace {
   float row[3][4];     // row r = (W[0][r], W[1][r], W[2][r], W[3][r]) of world_to_local
-  uint32_t blas_root;  // index into the BLAS root table
-  uint32_t leaf_count; // TLAS leaf length if this instance starts a TLAS leaf
+  uint32_t blas_root;  // root of the instance's BLAS in the wide BLAS node array
+  uint32_t ref_index;  // TLAS-permuted instance index of the reference (reported by hits)
   uint32_t pad[2];
 };
 struct alignas(16) GpuInstShade {
@@ -67,8 +53,22 @@ struct alignas(16) GpuVAttr {
   float t[3];
   float pad;
 };
-static_assert(sizeof(GpuNode) == 64, "GpuNode");
-static_assert(sizeof(GpuRoot) == 32, "GpuRoot");
+// 8-wide node collapsed from the reference's binary tree (80 B = 5 x 16 B).  Child boxes are
+// quantised to 8 bits per plane on a per-axis power-of-two grid anchored at p; the quantised
+// boxes contain the exact ones.  meta[k]: 0 = empty slot; 0x80 | r = inner child at
+// child_base + r; (n << 5) | o = leaf of n (1..3) primitives at prim_base + o.
+struct alignas(16) WideNode {
+  float p[3];
+  uint8_t e[3];        // biased exponent of the grid step per axis (float bits e << 23)
+  uint8_t n_children;
+  uint32_t child_base;
+  uint32_t prim_base;
+  uint8_t meta[8];
+  uint8_t qlo_x[8], qlo_y[8], qlo_z[8], qhi_x[8], qhi_y[8], qhi_z[8];
+};
+static_assert(sizeof(WideNode) == 80, "WideNode");
+constexpr uint32_t kInstanceBit = 0x80000000u;  // TLAS stack entry that names an instance
+
 static_assert(sizeof(GpuTri) == 48, "GpuTri");
 static_assert(sizeof(GpuInstTrace) == 64, "GpuInstTrace");
 static_assert(sizeof(GpuInstShade) == 96, "GpuInstShade");
@@ -82,10 +82,10 @@ struct HostScene {
   std::vector<nb_bvh_node> blas, tlas;
   std::vector<nb_instance> instances;  // TLAS-permuted
 
-  std::vector<GpuNode> gblas, gtlas;
-  GpuRoot tlas_root{};
+  std::vector<WideNode> wblas, wtlas;  // 8-wide trees; the TLAS root is wtlas[0]
+  std::vector<uint32_t> wblas_root;    // per distinct BLAS root: index of its root in wblas
+  size_t wblas_nodes = 0, wtlas_nodes = 0;  // sizes kept after the host copies are dropped
   bool has_tlas = false;
-  std::vector<GpuRoot> blas_roots;
   std::vector<GpuInstTrace> itrace;
   std::vector<GpuInstShade> ishade;
   std::vector<GpuTri> tris;

@@ -4,17 +4,23 @@
 // traversal inline (pathtracing.wgsl:161-260).  Here the pass is a wavefront:
 //   raygen      one path per (pixel, sample) of a batch: Cranley-Patterson-rotated Sobol
 //               jitter and generate_ray (pathtracing.wgsl:27-41, 245-255)
-//   trace       persistent warps pull 32-ray chunks with one atomic each and run the
-//               two-level stack traversal (raytracing_sw.wgsl:176-319) on the device layout
+//   trace       persistent warps take 32 rays at a time with one atomic and walk 8-wide
+//               quantised trees collapsed from the reference's TLAS/BLAS (raytracing_sw.wgsl:
+//               176-319): one 80-byte node load tests eight child boxes, leaf triangles are
+//               tested as soon as their box is hit, and hit children are pushed in distance
+//               order so the nearest is visited next
 //   shade       hit attributes (raytracing_sw.wgsl:138-173), env/emission termination, lobe
 //               choice, VNDF / cosine sampling, Russian roulette (pathtracing.wgsl:161-241);
 //               survivors are appended to the next bounce's queue with warp-aggregated atomics
 //   accumulate  running mean over the batch's samples in sample order (pathtracing.wgsl:258)
-// so traversal runs in a lean kernel at full occupancy and the path state lives in HBM.
+// so traversal runs in a lean kernel and the path state lives in HBM.
 //
-// Traversal differs from the reference in two work-saving ways that leave results unchanged
-// except for near-ties: the current closest hit prunes BLAS nodes (the reference restarts
-// each BLAS from NO_HIT, raytracing_sw.wgsl:255) and one stack serves both levels.
+// The traversal finds the reference's closest hit: quantised boxes contain the reference
+// boxes, triangles are tested with the reference's Moller-Trumbore arithmetic, and a hit
+// replaces the current one only when strictly closer.  Visiting order differs from the
+// reference (8-wide nodes, BLAS nodes pruned by the running closest hit where the reference
+// restarts each BLAS from NO_HIT, raytracing_sw.wgsl:255), so among triangles at exactly the
+// same distance another one may win: the documented near-tie class.
 
 #include <algorithm>
 #include <cstdint>
@@ -30,20 +36,19 @@ using nb::PathBatch;
 
 constexpr int kStackSize = 64;
 constexpr uint32_t kIterationCap = 1u << 22;
+constexpr uint32_t kInstanceBit = 0x80000000u;
+// t-space slack of the quantised slab test: covers the rounding of the fused plane
+// evaluation so that a box never rejects a ray the exact reference box accepts
+constexpr float kFarSlack = 1.0000004f;
 
 __device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
+__device__ __forceinline__ uint32_t f2u(float x) { return __float_as_uint(x); }
 
-// slab test (raytracing_sw.wgsl:81-89)
-__device__ __forceinline__ float slab(V3 ro, V3 rinv, float mnx, float mxx, float mny, float mxy, float mnz,
-                                      float mxz) {
-  float tminx = (mnx - ro.x) * rinv.x, tmaxx = (mxx - ro.x) * rinv.x;
-  float tminy = (mny - ro.y) * rinv.y, tmaxy = (mxy - ro.y) * rinv.y;
-  float tminz = (mnz - ro.z) * rinv.z, tmaxz = (mxz - ro.z) * rinv.z;
-  float t1x = fminf(tminx, tmaxx), t1y = fminf(tminy, tmaxy), t1z = fminf(tminz, tmaxz);
-  float t2x = fmaxf(tminx, tmaxx), t2y = fmaxf(tminy, tmaxy), t2z = fmaxf(tminz, tmaxz);
-  float tn = fmaxf(t1x, fmaxf(t1y, t1z));
-  float tf = fminf(t2x, fminf(t2y, t2z));
-  return (tn <= tf && tf >= 0.0f) ? tn : kNoHit;
+// direction reciprocal for box tests: components below 1e-20 in magnitude are nudged to
+// +-1e-20 so that every plane distance stays finite (triangle tests use the true direction)
+__device__ __forceinline__ float safe_rcp(float d) {
+  const float m = 1e-20f;
+  return 1.0f / (fabsf(d) < m ? copysignf(m, d) : d);
 }
 
 struct Hit {
@@ -51,199 +56,193 @@ struct Hit {
   uint32_t tri, inst;
 };
 
-// Traversal state of one lane (one ray) in the persistent kernels.  The stack lives in
-// local memory; everything else stays in registers.
-struct Lane {
-  V3 wo, wd, winv;  // world ray
-  V3 ro, rd, rinv;  // ray of the current level (world, or instance-local inside a BLAS)
-  Hit h;
-  int sp, blas_base;
-  uint32_t inst_cur, inst_end, cur_inst;
-  uint32_t ray, iter;
-  bool in_blas;
-};
-
-__device__ __forceinline__ void push(Lane& L, uint2* stack, uint32_t ref, float d, uint32_t& status) {
-  if (L.sp < kStackSize) {
-    stack[L.sp] = make_uint2(ref, __float_as_uint(d));
-    ++L.sp;
-  } else {
-    status |= kStatusStackOverflow;
-  }
-}
-
-// Enter the BLAS of instance j: transform the world ray (raytracing_sw.wgsl:202-206), test
-// the BLAS root box and push the root (raytracing_sw.wgsl:259-265).
-__device__ __forceinline__ void enter_instance(const DevScene& s, Lane& L, uint2* stack, uint32_t j,
-                                               uint32_t& status) {
-  const float4* it = s.inst_trace + 4 * (size_t)j;
-  const float4 r0 = ld4(it), r1 = ld4(it + 1), r2 = ld4(it + 2);
-  const uint32_t root = __float_as_uint(ld4(it + 3).x);
-  const V3 wo = L.wo, wd = L.wd;
-  L.ro = V3{r0.x * wo.x + r0.y * wo.y + r0.z * wo.z + r0.w * 1.0f, r1.x * wo.x + r1.y * wo.y + r1.z * wo.z + r1.w * 1.0f,
-            r2.x * wo.x + r2.y * wo.y + r2.z * wo.z + r2.w * 1.0f};
-  L.rd = V3{r0.x * wd.x + r0.y * wd.y + r0.z * wd.z, r1.x * wd.x + r1.y * wd.y + r1.z * wd.z,
-            r2.x * wd.x + r2.y * wd.y + r2.z * wd.z};
-  L.rinv = rcp3(L.rd);
-  L.cur_inst = j;
-  const float4 lo = ld4(s.blas_roots + 2 * (size_t)root), hi = ld4(s.blas_roots + 2 * (size_t)root + 1);
-  const float d = slab(L.ro, L.rinv, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
-  if (d < L.h.t) push(L, stack, __float_as_uint(lo.w), d, status);
-}
-
-// Start a new ray: test the TLAS root and push it (raytracing_sw.wgsl:182-191).
-__device__ __forceinline__ void lane_start(const DevScene& s, Lane& L, uint2* stack, V3 o, V3 d, uint32_t& status) {
-  L.wo = o; L.wd = d; L.winv = rcp3(d);
-  L.ro = o; L.rd = d; L.rinv = L.winv;
-  L.h.t = kNoHit; L.h.u = 0.0f; L.h.v = 0.0f; L.h.tri = 0xFFFFFFFFu; L.h.inst = 0xFFFFFFFFu;
-  L.sp = 0; L.blas_base = 0; L.in_blas = false; L.iter = 0;
-  L.inst_cur = L.inst_end = L.cur_inst = 0;
-  if (!s.has_tlas) return;
-  const float4 lo = s.tlas_root_lo, hi = s.tlas_root_hi;
-  const float dr = slab(o, L.winv, lo.x, hi.x, lo.y, hi.y, lo.z, hi.z);
-  if (dr < L.h.t) push(L, stack, __float_as_uint(lo.w), dr, status);
-}
-
-// One stack pop of the two-level traversal.  Returns true when the ray is finished.
+// Closest (or any) hit of one world-space ray.  Returns the status bits it raised.
 template <bool kAny>
-__device__ __forceinline__ bool lane_step(const DevScene& s, Lane& L, uint2* stack, uint32_t& status) {
-  if (++L.iter > kIterationCap) {
-    status |= kStatusIterationCap;
-    return true;
-  }
-  if (L.in_blas && L.sp == L.blas_base) {
-    if (L.inst_cur < L.inst_end) {  // next instance of the TLAS leaf (raytracing_sw.wgsl:201)
-      enter_instance(s, L, stack, L.inst_cur++, status);
-      return false;
+__device__ __forceinline__ uint32_t trace_ray(const DevScene& s, const V3 wo, const V3 wd, Hit& h) {
+  h.t = kNoHit;
+  h.u = h.v = 0.0f;
+  h.tri = 0xFFFFFFFFu;
+  h.inst = 0xFFFFFFFFu;
+  if (!s.has_tlas) return 0;
+  uint32_t status = 0;
+  const V3 winv{safe_rcp(wd.x), safe_rcp(wd.y), safe_rcp(wd.z)};
+  V3 ro = wo, rd = wd, rinv = winv;
+  uint2 stack[kStackSize];
+  int sp = 0, blas_base = 0;
+  bool in_blas = false;
+  uint32_t cur_inst = 0;
+  uint32_t node = 0;  // the TLAS root
+  bool have_node = true;
+  for (uint32_t iter = 0;; ++iter) {
+    if (iter > kIterationCap) {
+      status |= kStatusIterationCap;
+      break;
     }
-    L.in_blas = false;
-    L.ro = L.wo; L.rd = L.wd; L.rinv = L.winv;
-  }
-  if (L.sp == 0) return true;
-  --L.sp;
-  const uint2 e = stack[L.sp];
-  if (__uint_as_float(e.y) >= L.h.t) return false;  // raytracing_sw.wgsl:197,271
-  const uint32_t ref = e.x;
-  if (ref & kLeafBit) {
-    const uint32_t first = ref & ~kLeafBit;
-    if (!L.in_blas) {
-      // TLAS leaf: its instances one after the other (raytracing_sw.wgsl:200-217)
-      const uint32_t n = __float_as_uint(ld4(s.inst_trace + 4 * (size_t)first + 3).y);
-      L.inst_cur = first + 1;
-      L.inst_end = first + n;
-      L.in_blas = true;
-      L.blas_base = L.sp;
-      enter_instance(s, L, stack, first, status);
-      return false;
+    if (!have_node) {
+      bool done = false;
+      for (;;) {
+        if (in_blas && sp == blas_base) {  // BLAS finished: back to the world ray
+          in_blas = false;
+          ro = wo; rd = wd; rinv = winv;
+        }
+        if (sp == 0) {
+          done = true;
+          break;
+        }
+        --sp;
+        const uint2 e = stack[sp];
+        if (__uint_as_float(e.y) >= h.t) continue;  // raytracing_sw.wgsl:197,271
+        if (!in_blas && (e.x & kInstanceBit)) {
+          // enter an instance: transform the world ray (raytracing_sw.wgsl:202-206)
+          const float4* it = s.inst_trace + 4 * (size_t)(e.x & ~kInstanceBit);
+          const float4 r0 = ld4(it), r1 = ld4(it + 1), r2 = ld4(it + 2), r3 = ld4(it + 3);
+          ro = V3{r0.x * wo.x + r0.y * wo.y + r0.z * wo.z + r0.w * 1.0f,
+                  r1.x * wo.x + r1.y * wo.y + r1.z * wo.z + r1.w * 1.0f,
+                  r2.x * wo.x + r2.y * wo.y + r2.z * wo.z + r2.w * 1.0f};
+          rd = V3{r0.x * wd.x + r0.y * wd.y + r0.z * wd.z, r1.x * wd.x + r1.y * wd.y + r1.z * wd.z,
+                  r2.x * wd.x + r2.y * wd.y + r2.z * wd.z};
+          rinv = V3{safe_rcp(rd.x), safe_rcp(rd.y), safe_rcp(rd.z)};
+          node = f2u(r3.x);
+          cur_inst = f2u(r3.y);
+          in_blas = true;
+          blas_base = sp;
+        } else {
+          node = e.x;
+        }
+        break;
+      }
+      if (done) break;
     }
-    // BLAS leaf: Moller-Trumbore over the leaf's triangles (raytracing_sw.wgsl:51-78, 274-286)
-    const float4* tp = s.tris + 3 * (size_t)first;
-    float4 a = ld4(tp);
-    const uint32_t n = __float_as_uint(a.w);
-    for (uint32_t k = 0; k < n; ++k) {
-      if (k) a = ld4(tp + 3 * k);
-      const float4 b = ld4(tp + 3 * k + 1), c = ld4(tp + 3 * k + 2);
-      const V3 e1 = xyz(b), e2 = xyz(c);
-      const V3 hv = cross(L.rd, e2);
-      const float det = dot(e1, hv);
-      if (det < kEps) continue;
-      const float inv_det = 1.0f / det;
-      const V3 sv = L.ro - xyz(a);
-      const float u = inv_det * dot(sv, hv);
-      if (u < 0.0f || u > 1.0f) continue;
-      const V3 q = cross(sv, e1);
-      const float v = inv_det * dot(L.rd, q);
-      if (v < 0.0f || u + v > 1.0f) continue;
-      const float t = inv_det * dot(e2, q);
-      if (t < kBias) continue;
-      if (t < L.h.t) {
-        L.h.t = t; L.h.u = u; L.h.v = v;
-        L.h.tri = first + k;
-        L.h.inst = L.cur_inst;
-        if (kAny) return true;
+    have_node = false;
+
+    // ---- one 8-wide node: quantised slab tests of all children ----
+    const float4* np = (in_blas ? s.blas_wide : s.tlas_wide) + 5 * (size_t)node;
+    const float4 q0 = ld4(np), q1 = ld4(np + 1), q2 = ld4(np + 2), q3 = ld4(np + 3), q4 = ld4(np + 4);
+    const uint32_t eb = f2u(q0.w);
+    const float ax = __uint_as_float((eb & 0xFFu) << 23) * rinv.x;
+    const float ay = __uint_as_float(((eb >> 8) & 0xFFu) << 23) * rinv.y;
+    const float az = __uint_as_float(((eb >> 16) & 0xFFu) << 23) * rinv.z;
+    const float bx = (q0.x - ro.x) * rinv.x, by = (q0.y - ro.y) * rinv.y, bz = (q0.z - ro.z) * rinv.z;
+    const uint32_t child_base = f2u(q1.x), prim_base = f2u(q1.y);
+    const uint32_t m0 = f2u(q1.z), m1 = f2u(q1.w);
+    uint32_t key[8];
+    uint32_t leaf_mask = 0;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int sh = 8 * (k & 3);
+      const uint32_t meta = ((k < 4 ? m0 : m1) >> sh) & 0xFFu;
+      const float lx = (float)(((k < 4 ? f2u(q2.x) : f2u(q2.y)) >> sh) & 0xFFu);
+      const float ly = (float)(((k < 4 ? f2u(q2.z) : f2u(q2.w)) >> sh) & 0xFFu);
+      const float lz = (float)(((k < 4 ? f2u(q3.x) : f2u(q3.y)) >> sh) & 0xFFu);
+      const float hx = (float)(((k < 4 ? f2u(q3.z) : f2u(q3.w)) >> sh) & 0xFFu);
+      const float hy = (float)(((k < 4 ? f2u(q4.x) : f2u(q4.y)) >> sh) & 0xFFu);
+      const float hz = (float)(((k < 4 ? f2u(q4.z) : f2u(q4.w)) >> sh) & 0xFFu);
+      const float tlx = fmaf(lx, ax, bx), thx = fmaf(hx, ax, bx);
+      const float tly = fmaf(ly, ay, by), thy = fmaf(hy, ay, by);
+      const float tlz = fmaf(lz, az, bz), thz = fmaf(hz, az, bz);
+      const float tn = fmaxf(fmaxf(fminf(tlx, thx), fminf(tly, thy)), fminf(tlz, thz));
+      const float tf = fminf(fminf(fmaxf(tlx, thx), fmaxf(tly, thy)), fmaxf(tlz, thz)) * kFarSlack;
+      const bool hit = meta != 0u && tn <= tf && tf >= 0.0f && tn < h.t;
+      key[k] = 0xFFFFFFFFu;
+      if (hit) {
+        if (in_blas && !(meta & 0x80u)) leaf_mask |= 1u << k;
+        else key[k] = (f2u(fmaxf(tn, 0.0f)) & ~7u) | (uint32_t)k;
       }
     }
-    return false;
-  }
-  // inner node: test both children, push far then near (raytracing_sw.wgsl:218-247)
-  const float4* np = (L.in_blas ? s.blas_nodes : s.tlas_nodes) + 4 * (size_t)ref;
-  const float4 q0 = ld4(np), q1 = ld4(np + 1), q2 = ld4(np + 2), q3 = ld4(np + 3);
-  const float dl = slab(L.ro, L.rinv, q0.x, q0.y, q0.z, q0.w, q2.x, q2.y);
-  const float dr = slab(L.ro, L.rinv, q1.x, q1.y, q1.z, q1.w, q2.z, q2.w);
-  const uint32_t lref = __float_as_uint(q3.x), rref = __float_as_uint(q3.y);
-  uint32_t fref = lref, nref = rref;
-  float fd = dl, nd = dr;
-  if (dl < dr) { fref = rref; fd = dr; nref = lref; nd = dl; }
-  if (fd < L.h.t) push(L, stack, fref, fd, status);
-  if (nd < L.h.t) push(L, stack, nref, nd, status);
-  return false;
-}
 
-// Persistent traversal over rays [0, n): every lane whose ray finished takes the next ray
-// (one warp-aggregated atomic per refill), so warps stay full until the work runs out
-// instead of waiting for their slowest ray.
-constexpr uint32_t kFullMask = 0xFFFFFFFFu;
-template <bool kAny, class Io>
-__device__ __forceinline__ void trace_persistent(const DevScene& s, const Io& io, uint32_t n, uint32_t* fetch,
-                                                 uint32_t* status_out) {
-  const uint32_t lane = threadIdx.x & 31;
-  const uint32_t lt_mask = (1u << lane) - 1u;
-  uint2 stack[kStackSize];
-  Lane L;
-  bool active = false, retired = false;
-  uint32_t status = 0;
-  while (true) {
-    const bool want = !active && !retired;
-    const uint32_t wmask = __ballot_sync(kFullMask, want);
-    if (wmask) {
-      const int leader = __ffs(wmask) - 1;
-      uint32_t base = 0;
-      if ((int)lane == leader) base = atomicAdd(fetch, (uint32_t)__popc(wmask));
-      base = __shfl_sync(kFullMask, base, leader);
-      if (want) {
-        const uint32_t idx = base + (uint32_t)__popc(wmask & lt_mask);
-        if (idx < n) {
-          V3 o, d;
-          io.load(idx, o, d);
-          L.ray = idx;
-          lane_start(s, L, stack, o, d, status);
-          active = true;
-        } else {
-          retired = true;
+    // ---- BLAS leaves: Moller-Trumbore (raytracing_sw.wgsl:51-78, 274-286) ----
+    while (leaf_mask) {
+      const int k = __ffs(leaf_mask) - 1;
+      leaf_mask &= leaf_mask - 1;
+      const uint32_t meta = ((k < 4 ? m0 : m1) >> (8 * (k & 3))) & 0xFFu;
+      const uint32_t first = prim_base + (meta & 31u), n = meta >> 5;
+      for (uint32_t j = 0; j < n; ++j) {
+        const float4* tp = s.tris + 3 * (size_t)(first + j);
+        const float4 a = ld4(tp), b = ld4(tp + 1), c = ld4(tp + 2);
+        const V3 e1 = xyz(b), e2 = xyz(c);
+        const V3 hv = cross(rd, e2);
+        const float det = dot(e1, hv);
+        if (det < kEps) continue;
+        const float inv_det = 1.0f / det;
+        const V3 sv = ro - xyz(a);
+        const float u = inv_det * dot(sv, hv);
+        if (u < 0.0f || u > 1.0f) continue;
+        const V3 q = cross(sv, e1);
+        const float v = inv_det * dot(rd, q);
+        if (v < 0.0f || u + v > 1.0f) continue;
+        const float t = inv_det * dot(e2, q);
+        if (t < kBias) continue;
+        if (t < h.t) {
+          h.t = t; h.u = u; h.v = v;
+          h.tri = f2u(b.w);
+          h.inst = cur_inst;
+          if (kAny) return status;
         }
       }
     }
-    if (!__any_sync(kFullMask, active)) break;
-    if (active && lane_step<kAny>(s, L, stack, status)) {
-      io.store(L.ray, L.h);
-      active = false;
+
+    // ---- order hit children near to far (19-comparator network) ----
+#define NB_CX(i, j)                                  \
+  {                                                  \
+    const uint32_t lo_ = min(key[i], key[j]);        \
+    key[j] = max(key[i], key[j]);                    \
+    key[i] = lo_;                                    \
+  }
+    NB_CX(0, 2) NB_CX(1, 3) NB_CX(4, 6) NB_CX(5, 7)
+    NB_CX(0, 4) NB_CX(1, 5) NB_CX(2, 6) NB_CX(3, 7)
+    NB_CX(0, 1) NB_CX(2, 3) NB_CX(4, 5) NB_CX(6, 7)
+    NB_CX(2, 4) NB_CX(3, 5)
+    NB_CX(1, 4) NB_CX(3, 6)
+    NB_CX(1, 2) NB_CX(3, 4) NB_CX(5, 6)
+#undef NB_CX
+    // push far to near; the nearest inner child is visited next without a push
+#pragma unroll
+    for (int k = 7; k >= 0; --k) {
+      const uint32_t kk = key[k];
+      if (kk == 0xFFFFFFFFu) continue;
+      const float d = __uint_as_float(kk & ~7u);
+      if (d >= h.t) continue;  // a leaf tested above moved the closest hit
+      const uint32_t slot = kk & 7u;
+      const uint32_t meta = ((slot < 4 ? m0 : m1) >> (8 * (slot & 3))) & 0xFFu;
+      const uint32_t ref = (meta & 0x80u) ? child_base + (meta & 7u) : (kInstanceBit | (prim_base + (meta & 31u)));
+      if (k == 0 && (meta & 0x80u)) {
+        node = ref;
+        have_node = true;
+      } else if (sp < kStackSize) {
+        stack[sp] = make_uint2(ref, kk & ~7u);
+        ++sp;
+      } else {
+        status |= kStatusStackOverflow;
+      }
     }
   }
-  if (status) atomicOr(status_out, status);
+  return status;
 }
-
-struct QueryIo {  // caller rays of 8 floats (origin, pad, direction, pad)
-  const float4* rays;
-  float4* hits;
-  uint32_t* inst;
-  __device__ __forceinline__ void load(uint32_t i, V3& o, V3& d) const {
-    o = xyz(__ldg(rays + 2 * (size_t)i));
-    d = xyz(__ldg(rays + 2 * (size_t)i + 1));
-  }
-  __device__ __forceinline__ void store(uint32_t i, const Hit& h) const {
-    hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
-    if (inst) inst[i] = h.inst;
-  }
-};
 
 // ------------------------------------------------------------------------------------------
 // traversal-only query (nb_trace_rays)
 // ------------------------------------------------------------------------------------------
 template <bool kAny>
-__global__ void __launch_bounds__(128, 8) k_trace_rays(DevScene s, const float4* __restrict__ rays, uint32_t n,
+__global__ void __launch_bounds__(128) k_trace_rays(DevScene s, const float4* __restrict__ rays, uint32_t n,
                                                      float4* __restrict__ hits, uint32_t* __restrict__ inst,
                                                      uint32_t* __restrict__ fetch, uint32_t* __restrict__ status) {
-  trace_persistent<kAny>(s, QueryIo{rays, hits, inst}, n, fetch, status);
+  const int lane = threadIdx.x & 31;
+  uint32_t st = 0;
+  while (true) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(fetch, 32u);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (base >= n) break;
+    const uint32_t i = base + lane;
+    if (i < n) {
+      const float4 o = __ldg(rays + 2 * (size_t)i), d = __ldg(rays + 2 * (size_t)i + 1);
+      Hit h;
+      st |= trace_ray<kAny>(s, xyz(o), xyz(d), h);
+      hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
+      if (inst) inst[i] = h.inst;
+    }
+  }
+  if (st) atomicOr(status, st);
 }
 
 // ------------------------------------------------------------------------------------------
@@ -290,26 +289,28 @@ __global__ void __launch_bounds__(256) k_raygen(PathBatch pb, CameraParams cam) 
   }
 }
 
-struct WaveIo {  // the bounce's ray queue and hit buffers
-  const float4* qo;
-  const float4* qd;
-  float4* hits;
-  uint32_t* inst;
-  __device__ __forceinline__ void load(uint32_t i, V3& o, V3& d) const {
-    o = xyz(qo[i]);
-    d = xyz(qd[i]);
-  }
-  __device__ __forceinline__ void store(uint32_t i, const Hit& h) const {
-    hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
-    inst[i] = h.inst;
-  }
-};
-
-__global__ void __launch_bounds__(128, 8) k_trace_wave(DevScene s, PathBatch pb, uint32_t bounce,
+__global__ void __launch_bounds__(128) k_trace_wave(DevScene s, PathBatch pb, uint32_t bounce,
                                                     unsigned long long* __restrict__ ray_total) {
   const uint32_t n = pb.counts[bounce];
-  const WaveIo io{(bounce & 1) ? pb.q_o[1] : pb.q_o[0], (bounce & 1) ? pb.q_d[1] : pb.q_d[0], pb.hits, pb.hit_inst};
-  trace_persistent<false>(s, io, n, pb.fetch + bounce, pb.status);
+  const float4* __restrict__ qo = (bounce & 1) ? pb.q_o[1] : pb.q_o[0];
+  const float4* __restrict__ qd = (bounce & 1) ? pb.q_d[1] : pb.q_d[0];
+  const int lane = threadIdx.x & 31;
+  uint32_t st = 0;
+  while (true) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(pb.fetch + bounce, 32u);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (base >= n) break;
+    const uint32_t i = base + lane;
+    if (i < n) {
+      const float4 o = qo[i], d = qd[i];
+      Hit h;
+      st |= trace_ray<false>(s, xyz(o), xyz(d), h);
+      pb.hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
+      pb.hit_inst[i] = h.inst;
+    }
+  }
+  if (st) atomicOr(pb.status, st);
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(ray_total, (unsigned long long)n);
 }
 

@@ -7,10 +7,11 @@
 // traversal constant, MAX_DEPTH 32, explicit DFS stack (children appended at len, len+1;
 // right child processed first) and the unstable in-place swap partition.  Rust evaluates
 // f32 arithmetic without contraction; this file is compiled with -ffp-contract=off to match.
-// The one deliberate difference from the reference is parallelism: distinct BLASes (disjoint
-// triangle ranges) are built on worker threads into private node lists that are then
-// concatenated in primitive order with their indices offset, which yields the same array
-// as the sequential appends.
+// The one deliberate difference from the reference is parallelism, at two levels, both with
+// an identical result: distinct BLASes (disjoint triangle ranges) are built on worker threads
+// into private node lists that are concatenated in primitive order with their indices
+// offset, and large subtrees inside one BLAS are split on separate threads, after which the
+// reference's node numbering is replayed (append_tree_parallel).
 
 #include <algorithm>
 #include <atomic>
@@ -18,6 +19,7 @@
 #include <cmath>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <thread>
 #include <utility>
 
@@ -211,6 +213,62 @@ uint32_t append_tree(std::vector<nb_bvh_node>& nodes, Prim* p, uint32_t s, uint3
   return root;
 }
 
+// Parallel form of append_tree with an identical result.  A node's split depends only on the
+// primitives of its own range, and sibling ranges are disjoint, so subtrees above a size
+// threshold are split on separate threads.  The reference numbers nodes in the order its
+// right-first DFS splits them (children at len, len + 1); replaying that DFS over the finished
+// structure reproduces the numbering, and the in-place partitions leave the same permutation.
+struct TreeNode {
+  nb_bvh_node n;
+  std::unique_ptr<TreeNode> lo, hi;
+};
+
+void split_recursive(Prim* p, TreeNode* t, uint32_t depth, int spawn_depth) {
+  constexpr uint32_t kMaxDepth = 32;
+  constexpr uint32_t kParallelMin = 1u << 15;
+  if (depth >= kMaxDepth) return;
+  nb_bvh_node lo, hi;
+  if (!split_node(p, t->n, &lo, &hi)) return;
+  t->lo.reset(new TreeNode{lo, nullptr, nullptr});
+  t->hi.reset(new TreeNode{hi, nullptr, nullptr});
+  if (spawn_depth > 0 && lo.end - lo.start >= kParallelMin && hi.end - hi.start >= kParallelMin) {
+    std::thread th(split_recursive, p, t->lo.get(), depth + 1, spawn_depth - 1);
+    split_recursive(p, t->hi.get(), depth + 1, spawn_depth - 1);
+    th.join();
+  } else {
+    split_recursive(p, t->lo.get(), depth + 1, spawn_depth);
+    split_recursive(p, t->hi.get(), depth + 1, spawn_depth);
+  }
+}
+
+uint32_t append_tree_parallel(std::vector<nb_bvh_node>& nodes, Prim* p, uint32_t s, uint32_t e, int spawn_depth) {
+  TreeNode root{leaf_over(p, s, e), nullptr, nullptr};
+  split_recursive(p, &root, 0, spawn_depth);
+  uint32_t root_index = (uint32_t)nodes.size();
+  nodes.push_back(root.n);
+  std::vector<std::pair<const TreeNode*, uint32_t>> stack{{&root, root_index}};
+  while (!stack.empty()) {
+    auto [t, idx] = stack.back();
+    stack.pop_back();
+    if (!t->lo) continue;
+    uint32_t li = (uint32_t)nodes.size();
+    nodes[idx].end = 0;
+    nodes[idx].start = li;
+    nodes.push_back(t->lo->n);
+    nodes.push_back(t->hi->n);
+    stack.emplace_back(t->lo.get(), li);
+    stack.emplace_back(t->hi.get(), li + 1);
+  }
+  return root_index;
+}
+
+int spawn_depth_for(uint32_t n) {
+  unsigned hw = std::max(1u, std::thread::hardware_concurrency());
+  int d = 0;
+  while ((1u << d) < hw && d < 6) ++d;
+  return n >= (1u << 16) ? d : 0;
+}
+
 void triangle_cache(const float* pos, size_t pos_stride, const uint32_t* idx, size_t nt, Prim* out) {
   for (size_t t = 0; t < nt; ++t) {
     const float* a = pos + pos_stride * idx[3 * t];
@@ -274,7 +332,7 @@ int build_bvh_triangles(const float* positions, size_t n_vertices, const uint32_
   std::vector<Prim> tris(nt);
   triangle_cache(positions, 3, indices, nt, tris.data());
   nodes->clear();
-  if (nt) append_tree(*nodes, tris.data(), 0, (uint32_t)nt);
+  if (nt) append_tree_parallel(*nodes, tris.data(), 0, (uint32_t)nt, spawn_depth_for((uint32_t)nt));
   permuted->assign(indices, indices + n_indices);
   for (size_t t = 0; t < nt; ++t)
     for (int k = 0; k < 3; ++k) (*permuted)[3 * t + k] = indices[3 * tris[t].payload + k];
@@ -319,7 +377,8 @@ int build_scene_reference(const nb_vertex* vertices, size_t nv, const uint32_t* 
     const std::vector<size_t>& members = g.second;
     size_t reps = dedup ? 1 : members.size();
     for (size_t r = 0; r < reps; ++r)
-      append_tree(local[members[r]], tris.data(), g.first.first, g.first.second);
+      append_tree_parallel(local[members[r]], tris.data(), g.first.first, g.first.second,
+                           spawn_depth_for(g.first.second - g.first.first));
   };
   if (disjoint) {
     // largest ranges first so the pool stays busy
@@ -420,76 +479,247 @@ int adopt_reference_buffers(const nb_bvh_node* blas, size_t n_blas, const nb_bvh
 
 namespace {
 
-// Translates one reference tree into GpuNodes (preorder, left subtree first).  Returns the
-// root reference; sets leaf lengths through `mark_leaf`.
-template <class MarkLeaf>
-int translate_tree(const std::vector<nb_bvh_node>& ref, uint32_t root, size_t n_prims, std::vector<GpuNode>* gpu,
-                   std::vector<int64_t>* gpu_index, MarkLeaf&& mark_leaf, uint32_t* root_ref, uint32_t* depth_out) {
-  auto ref_of = [&](uint32_t n, uint32_t* word) -> int {
+// ---------------------------------------------------------------------------------------
+// 8-wide device trees
+//
+// Each reference tree is collapsed top-down: a wide node starts from the two children of a
+// binary node and repeatedly replaces its largest-area expandable item (an inner binary node,
+// or a leaf of more than 3 primitives, split in two contiguous halves) by its two halves
+// until it holds 8 items.  Items that remain inner binary nodes or oversized leaves become
+// child wide nodes; leaves of at most 3 primitives become leaf slots.  Nodes are emitted
+// breadth-first so the inner children of a node are contiguous, and the primitives of a
+// node's leaf slots are written contiguously, in slot order, into a new primitive order.
+// Traversal finds the same closest hit: the wide tree covers the same primitives with boxes
+// that contain the reference boxes; only the visiting order (exact-t ties) can differ.
+// ---------------------------------------------------------------------------------------
+struct Item {
+  bool inner;       // inner binary node (else: primitive range)
+  uint32_t node;    // binary node index (inner)
+  uint32_t start, count;
+  double mn[3], mx[3];
+  double area() const {
+    double e0 = mx[0] - mn[0], e1 = mx[1] - mn[1], e2 = mx[2] - mn[2];
+    return e0 * e1 + e0 * e2 + e1 * e2;
+  }
+};
+
+struct Collapser {
+  const std::vector<nb_bvh_node>& ref;
+  // primitive boxes (float), indexed by reference primitive index
+  const std::vector<float>& prim_box;  // 6 floats per primitive: min xyz, max xyz
+  std::vector<WideNode>* out;
+  std::vector<uint32_t>* prim_order;   // new order -> reference primitive index
+  uint32_t max_leaf;                   // primitives per leaf slot (3 triangles, 1 instance)
+
+  Item item_of(uint32_t n) const {
+    const nb_bvh_node& b = ref[n];
+    Item it{};
+    it.inner = b.end == 0;
+    it.node = n;
+    it.start = b.start;
+    it.count = b.end > 0 ? b.end - b.start : 0;
+    for (int k = 0; k < 3; ++k) { it.mn[k] = b.min[k]; it.mx[k] = b.max[k]; }
+    return it;
+  }
+  Item range_item(uint32_t start, uint32_t count) const {
+    Item it{};
+    it.inner = false;
+    it.start = start;
+    it.count = count;
+    for (int k = 0; k < 3; ++k) { it.mn[k] = INFINITY; it.mx[k] = -INFINITY; }
+    for (uint32_t i = start; i < start + count; ++i)
+      for (int k = 0; k < 3; ++k) {
+        it.mn[k] = std::min(it.mn[k], (double)prim_box[6 * (size_t)i + k]);
+        it.mx[k] = std::max(it.mx[k], (double)prim_box[6 * (size_t)i + 3 + k]);
+      }
+    return it;
+  }
+  bool expandable(const Item& it) const { return it.inner || it.count > max_leaf; }
+  void expand(const Item& it, std::vector<Item>* v) const {
+    if (it.inner) {
+      v->push_back(item_of(ref[it.node].start));
+      v->push_back(item_of(ref[it.node].start + 1));
+    } else {
+      uint32_t h = it.count / 2;
+      v->push_back(range_item(it.start, h));
+      v->push_back(range_item(it.start + h, it.count - h));
+    }
+  }
+
+  // quantise child boxes of one wide node on a per-axis power-of-two grid
+  static void quantise(WideNode* w, const std::vector<Item>& slots) {
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (const Item& c : slots)
+      for (int k = 0; k < 3; ++k) { lo[k] = std::min(lo[k], c.mn[k]); hi[k] = std::max(hi[k], c.mx[k]); }
+    uint8_t* qlo[3] = {w->qlo_x, w->qlo_y, w->qlo_z};
+    uint8_t* qhi[3] = {w->qhi_x, w->qhi_y, w->qhi_z};
+    for (int k = 0; k < 3; ++k) {
+      // p rounded down so that p <= every child's min
+      float p = (float)lo[k];
+      if ((double)p > lo[k]) p = std::nextafter(p, -INFINITY);
+      double ext = hi[k] - (double)p;
+      int e = ext > 0.0 ? (int)std::ceil(std::log2(ext / 255.0)) : -100;
+      e = std::max(e, -126);
+      for (;; ++e) {
+        double scale = std::ldexp(1.0, e);
+        bool ok = true;
+        for (size_t i = 0; i < slots.size() && ok; ++i) {
+          double ql = std::floor((slots[i].mn[k] - p) / scale);
+          double qh = std::ceil((slots[i].mx[k] - p) / scale);
+          while (ql > 0 && p + ql * scale > slots[i].mn[k]) ql -= 1;
+          while (p + qh * scale < slots[i].mx[k]) qh += 1;
+          if (ql < 0 || qh > 255) { ok = false; break; }
+          qlo[k][i] = (uint8_t)ql;
+          qhi[k][i] = (uint8_t)qh;
+        }
+        if (ok) break;
+      }
+      w->p[k] = p;
+      w->e[k] = (uint8_t)(e + 127);
+    }
+  }
+
+  // builds the wide tree rooted at binary node `root`; returns the index of its root
+  uint32_t build(uint32_t root) {
+    std::vector<Item> queue;
+    size_t head = 0;
+    uint32_t base = (uint32_t)out->size();
+    Item r = item_of(root);
+    queue.push_back(r);
+    out->push_back(WideNode{});
+    while (head < queue.size()) {
+      const Item cur = queue[head];
+      const uint32_t self = base + (uint32_t)head;
+      ++head;
+      std::vector<Item> items;
+      if (cur.inner) expand(cur, &items);
+      else items.push_back(cur);
+      while (items.size() < 8) {
+        int best = -1;
+        double best_area = -1.0;
+        for (size_t i = 0; i < items.size(); ++i)
+          if (expandable(items[i]) && items[i].area() > best_area) { best = (int)i; best_area = items[i].area(); }
+        if (best < 0) break;
+        Item it = items[best];
+        items.erase(items.begin() + best);
+        expand(it, &items);
+      }
+      WideNode w{};
+      std::vector<Item> slots;
+      w.child_base = (uint32_t)out->size();
+      w.prim_base = (uint32_t)prim_order->size();
+      uint32_t n_inner = 0, offset = 0;
+      for (const Item& it : items) {
+        uint8_t meta;
+        if (expandable(it)) {
+          meta = (uint8_t)(0x80u | n_inner);
+          ++n_inner;
+          queue.push_back(it);
+          out->push_back(WideNode{});
+        } else {
+          meta = (uint8_t)((it.count << 5) | offset);
+          for (uint32_t i = it.start; i < it.start + it.count; ++i) prim_order->push_back(i);
+          offset += it.count;
+        }
+        w.meta[slots.size()] = meta;
+        slots.push_back(it);
+      }
+      w.n_children = (uint8_t)slots.size();
+      quantise(&w, slots);
+      (*out)[self] = w;
+    }
+    return base;
+  }
+};
+
+void tri_boxes(const HostScene& s, std::vector<float>* box) {
+  size_t nt = s.indices.size() / 3;
+  box->resize(6 * nt);
+  for (size_t t = 0; t < nt; ++t) {
+    const float* a = s.vertices[s.indices[3 * t]].position;
+    const float* b = s.vertices[s.indices[3 * t + 1]].position;
+    const float* c = s.vertices[s.indices[3 * t + 2]].position;
+    for (int k = 0; k < 3; ++k) {
+      (*box)[6 * t + k] = std::min(std::min(a[k], b[k]), c[k]);
+      (*box)[6 * t + 3 + k] = std::max(std::max(a[k], b[k]), c[k]);
+    }
+  }
+}
+
+int check_tree(const std::vector<nb_bvh_node>& ref, uint32_t root, size_t n_prims) {
+  if (root >= ref.size()) return fail(NB_ERR_INVALID_ARG, "root %u out of range", root);
+  std::vector<std::pair<uint32_t, uint32_t>> stack{{root, 0u}};
+  size_t visited = 0;
+  while (!stack.empty()) {
+    auto [n, d] = stack.back();
+    stack.pop_back();
+    if (++visited > 2 * ref.size() + 2) return fail(NB_ERR_INVALID_ARG, "BVH contains a cycle");
     const nb_bvh_node& node = ref[n];
     if (node.end > 0) {
       if (node.start >= node.end || node.end > n_prims || node.start >= kLeafBit)
         return fail(NB_ERR_INVALID_ARG, "leaf node %u covers an invalid range [%u, %u)", n, node.start, node.end);
-      int st = mark_leaf(node.start, node.end - node.start);
-      if (st) return st;
-      *word = kLeafBit | node.start;
-      return NB_OK;
+      continue;
     }
-    if ((*gpu_index)[n] < 0) return fail(NB_ERR_INVALID_ARG, "internal: unassigned node %u", n);
-    *word = (uint32_t)(*gpu_index)[n];
-    return NB_OK;
-  };
-  if (root >= ref.size()) return fail(NB_ERR_INVALID_ARG, "root %u out of range", root);
-  uint32_t max_depth = 0;
-  // assign indices in preorder, then fill records
-  std::vector<std::pair<uint32_t, uint32_t>> stack{{root, 0u}};
-  std::vector<uint32_t> order;
-  while (!stack.empty()) {
-    auto [n, d] = stack.back();
-    stack.pop_back();
-    max_depth = std::max(max_depth, d);
-    const nb_bvh_node& node = ref[n];
-    if (node.end > 0) continue;
-    if ((*gpu_index)[n] >= 0) continue;  // shared subtree already translated
     if (d > 64) return fail(NB_ERR_INVALID_ARG, "BVH deeper than 64 levels");
     if ((size_t)node.start + 1 >= ref.size()) return fail(NB_ERR_INVALID_ARG, "inner node %u: child out of range", n);
-    (*gpu_index)[n] = (int64_t)(gpu->size() + order.size());
-    order.push_back(n);
-    stack.emplace_back(node.start + 1, d + 1);
     stack.emplace_back(node.start, d + 1);
+    stack.emplace_back(node.start + 1, d + 1);
   }
-  size_t base = gpu->size();
-  gpu->resize(base + order.size());
-  for (size_t i = 0; i < order.size(); ++i) {
-    const nb_bvh_node& node = ref[order[i]];
-    const nb_bvh_node& c0 = ref[node.start];
-    const nb_bvh_node& c1 = ref[node.start + 1];
-    GpuNode& g = (*gpu)[base + i];
-    g.q0[0] = c0.min[0]; g.q0[1] = c0.max[0]; g.q0[2] = c0.min[1]; g.q0[3] = c0.max[1];
-    g.q1[0] = c1.min[0]; g.q1[1] = c1.max[0]; g.q1[2] = c1.min[1]; g.q1[3] = c1.max[1];
-    g.q2[0] = c0.min[2]; g.q2[1] = c0.max[2]; g.q2[2] = c1.min[2]; g.q2[3] = c1.max[2];
-    int st = ref_of(node.start, &g.ref[0]);
-    if (!st) st = ref_of(node.start + 1, &g.ref[1]);
-    if (st) return st;
-    g.pad[0] = g.pad[1] = 0;
+  return NB_OK;
+}
+
+// world box of an instance: the 8 corners of its BLAS root box through local_to_world
+// (InstanceWithBounds::approximate_from_instance, scene.rs:239-259)
+void instance_box(const nb_instance& in, const nb_bvh_node& r, float* box) {
+  float wmn[3] = {INFINITY, INFINITY, INFINITY}, wmx[3] = {-INFINITY, -INFINITY, -INFINITY};
+  for (int c = 0; c < 8; ++c) {
+    float l[3] = {(c & 1) ? r.max[0] : r.min[0], (c & 2) ? r.max[1] : r.min[1], (c & 4) ? r.max[2] : r.min[2]};
+    float w[3];
+    transform_point3(in.local_to_world, l, w);
+    for (int q = 0; q < 3; ++q) { wmn[q] = min_num(wmn[q], w[q]); wmx[q] = max_num(wmx[q], w[q]); }
   }
-  int st = ref_of(root, root_ref);
-  if (depth_out) *depth_out = max_depth;
-  return st;
+  for (int q = 0; q < 3; ++q) { box[q] = wmn[q]; box[3 + q] = wmx[q]; }
 }
 
 }  // namespace
 
 int to_device_layout(HostScene* s) {
-  size_t nt = s->indices.size() / 3;
-  size_t nv = s->vertices.size();
-  s->tris.assign(nt, GpuTri{});
-  for (size_t t = 0; t < nt; ++t) {
+  const size_t nt = s->indices.size() / 3;
+  const size_t nv = s->vertices.size();
+  const size_t n_inst = s->instances.size();
+  std::vector<float> tbox;
+  tri_boxes(*s, &tbox);
+
+  // BLAS: one wide tree per distinct root; triangles re-ordered per wide tree
+  s->wblas.clear();
+  s->wblas_root.clear();
+  std::vector<uint32_t> tri_order;
+  std::map<uint32_t, uint32_t> root_id;
+  Collapser cb{s->blas, tbox, &s->wblas, &tri_order, 3};
+  std::vector<uint32_t> inst_blas(n_inst);
+  for (size_t i = 0; i < n_inst; ++i) {
+    const uint32_t root = s->instances[i].node;
+    auto it = root_id.find(root);
+    if (it == root_id.end()) {
+      int st = check_tree(s->blas, root, nt);
+      if (st) return st;
+      uint32_t id = (uint32_t)s->wblas_root.size();
+      s->wblas_root.push_back(cb.build(root));
+      it = root_id.emplace(root, id).first;
+    }
+    inst_blas[i] = it->second;
+  }
+  s->tris.assign(tri_order.size(), GpuTri{});
+  for (size_t k = 0; k < tri_order.size(); ++k) {
+    const uint32_t t = tri_order[k];
     const float* a = s->vertices[s->indices[3 * t]].position;
     const float* b = s->vertices[s->indices[3 * t + 1]].position;
     const float* c = s->vertices[s->indices[3 * t + 2]].position;
-    GpuTri& g = s->tris[t];
-    for (int k = 0; k < 3; ++k) { g.v0[k] = a[k]; g.e1[k] = b[k] - a[k]; g.e2[k] = c[k] - a[k]; }
+    GpuTri& g = s->tris[k];
+    for (int q = 0; q < 3; ++q) { g.v0[q] = a[q]; g.e1[q] = b[q] - a[q]; g.e2[q] = c[q] - a[q]; }
+    g.pad0 = 0;
+    g.ref_index = t;
+    g.pad2 = 0;
   }
   s->vattr.resize(nv);
   for (size_t i = 0; i < nv; ++i) {
@@ -499,41 +729,33 @@ int to_device_layout(HostScene* s) {
     g.tw = v.tangent[3];
     g.pad = 0.0f;
   }
-  // BLAS trees, one root table entry per distinct root node
-  s->gblas.clear();
-  s->blas_roots.clear();
-  std::vector<int64_t> gidx(s->blas.size(), -1);
-  std::map<uint32_t, uint32_t> root_id;
-  auto mark_tri = [&](uint32_t start, uint32_t count) -> int {
-    uint32_t& lc = s->tris[start].leaf_count;
-    if (lc != 0 && lc != count)
-      return fail(NB_ERR_INVALID_ARG, "triangle %u starts two leaves of different length", start);
-    lc = count;
-    return NB_OK;
-  };
-  size_t n_inst = s->instances.size();
-  s->itrace.assign(n_inst, GpuInstTrace{});
+
+  // TLAS over instances (boxes from their BLAS roots), instances re-ordered by the wide TLAS
+  s->wtlas.clear();
+  s->itrace.clear();
   s->ishade.assign(n_inst, GpuInstShade{});
-  for (size_t i = 0; i < n_inst; ++i) {
+  s->has_tlas = !s->tlas.empty() && n_inst > 0;
+  std::vector<uint32_t> inst_order;
+  if (s->has_tlas) {
+    int st = check_tree(s->tlas, 0, n_inst);
+    if (st) return st;
+    std::vector<float> ibox(6 * n_inst);
+    for (size_t i = 0; i < n_inst; ++i) instance_box(s->instances[i], s->blas[s->instances[i].node], &ibox[6 * i]);
+    Collapser ct{s->tlas, ibox, &s->wtlas, &inst_order, 1};
+    ct.build(0);  // raytracing_sw.wgsl:183-186: the TLAS root is node 0
+  }
+  s->itrace.assign(inst_order.size(), GpuInstTrace{});
+  for (size_t k = 0; k < inst_order.size(); ++k) {
+    const uint32_t i = inst_order[k];
     const nb_instance& in = s->instances[i];
-    auto it = root_id.find(in.node);
-    uint32_t id;
-    if (it == root_id.end()) {
-      GpuRoot r{};
-      const nb_bvh_node& rn = s->blas[in.node];
-      for (int k = 0; k < 3; ++k) { r.mn[k] = rn.min[k]; r.mx[k] = rn.max[k]; }
-      int st = translate_tree(s->blas, in.node, nt, &s->gblas, &gidx, mark_tri, &r.ref, nullptr);
-      if (st) return st;
-      id = (uint32_t)s->blas_roots.size();
-      s->blas_roots.push_back(r);
-      root_id[in.node] = id;
-    } else {
-      id = it->second;
-    }
-    GpuInstTrace& tr = s->itrace[i];
+    GpuInstTrace& tr = s->itrace[k];
     for (int r = 0; r < 3; ++r)
       for (int c = 0; c < 4; ++c) tr.row[r][c] = in.world_to_local[4 * c + r];
-    tr.blas_root = id;
+    tr.blas_root = s->wblas_root[inst_blas[i]];
+    tr.ref_index = i;
+  }
+  for (size_t i = 0; i < n_inst; ++i) {
+    const nb_instance& in = s->instances[i];
     GpuInstShade& sh = s->ishade[i];
     for (int c = 0; c < 3; ++c) {
       for (int k = 0; k < 3; ++k) sh.w2l_col[c][k] = in.world_to_local[4 * c + k];
@@ -544,24 +766,6 @@ int to_device_layout(HostScene* s) {
     sh.l2w_row[0][3] = in.roughness;
     sh.l2w_row[1][3] = in.metallic;
     sh.l2w_row[2][3] = in.emissive;
-  }
-  // TLAS
-  s->gtlas.clear();
-  s->has_tlas = !s->tlas.empty() && n_inst > 0;
-  if (s->has_tlas) {
-    std::vector<int64_t> tidx(s->tlas.size(), -1);
-    auto mark_inst = [&](uint32_t start, uint32_t count) -> int {
-      uint32_t& lc = s->itrace[start].leaf_count;
-      if (lc != 0 && lc != count) return fail(NB_ERR_INVALID_ARG, "instance %u starts two TLAS leaves", start);
-      lc = count;
-      return NB_OK;
-    };
-    GpuRoot r{};
-    const nb_bvh_node& rn = s->tlas[0];  // raytracing_sw.wgsl:183-186: the TLAS root is node 0
-    for (int k = 0; k < 3; ++k) { r.mn[k] = rn.min[k]; r.mx[k] = rn.max[k]; }
-    int st = translate_tree(s->tlas, 0, n_inst, &s->gtlas, &tidx, mark_inst, &r.ref, nullptr);
-    if (st) return st;
-    s->tlas_root = r;
   }
   return NB_OK;
 }
