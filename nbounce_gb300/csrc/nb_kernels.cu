@@ -125,28 +125,39 @@ __device__ __forceinline__ uint32_t trace_ray(const DevScene& s, const V3 wo, co
     const float bx = (q0.x - ro.x) * rinv.x, by = (q0.y - ro.y) * rinv.y, bz = (q0.z - ro.z) * rinv.z;
     const uint32_t child_base = f2u(q1.x), prim_base = f2u(q1.y);
     const uint32_t m0 = f2u(q1.z), m1 = f2u(q1.w);
+    // near/far planes per axis by the sign of the direction: the near plane of a child is its
+    // low plane where rinv >= 0 (t grows with the quantised coordinate), else its high plane
+    const bool pxs = rinv.x >= 0.0f, pys = rinv.y >= 0.0f, pzs = rinv.z >= 0.0f;
+    const uint32_t nx0 = pxs ? f2u(q2.x) : f2u(q3.z), nx1 = pxs ? f2u(q2.y) : f2u(q3.w);
+    const uint32_t fx0 = pxs ? f2u(q3.z) : f2u(q2.x), fx1 = pxs ? f2u(q3.w) : f2u(q2.y);
+    const uint32_t ny0 = pys ? f2u(q2.z) : f2u(q4.x), ny1 = pys ? f2u(q2.w) : f2u(q4.y);
+    const uint32_t fy0 = pys ? f2u(q4.x) : f2u(q2.z), fy1 = pys ? f2u(q4.y) : f2u(q2.w);
+    const uint32_t nz0 = pzs ? f2u(q3.x) : f2u(q4.z), nz1 = pzs ? f2u(q3.y) : f2u(q4.w);
+    const uint32_t fz0 = pzs ? f2u(q4.z) : f2u(q3.x), fz1 = pzs ? f2u(q4.w) : f2u(q3.y);
     uint32_t key[8];
-    uint32_t leaf_mask = 0;
+    uint32_t leaf_mask = 0, n_push = 0;
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
-      const int sh = 8 * (k & 3);
-      const uint32_t meta = ((k < 4 ? m0 : m1) >> sh) & 0xFFu;
-      const float lx = (float)(((k < 4 ? f2u(q2.x) : f2u(q2.y)) >> sh) & 0xFFu);
-      const float ly = (float)(((k < 4 ? f2u(q2.z) : f2u(q2.w)) >> sh) & 0xFFu);
-      const float lz = (float)(((k < 4 ? f2u(q3.x) : f2u(q3.y)) >> sh) & 0xFFu);
-      const float hx = (float)(((k < 4 ? f2u(q3.z) : f2u(q3.w)) >> sh) & 0xFFu);
-      const float hy = (float)(((k < 4 ? f2u(q4.x) : f2u(q4.y)) >> sh) & 0xFFu);
-      const float hz = (float)(((k < 4 ? f2u(q4.z) : f2u(q4.w)) >> sh) & 0xFFu);
-      const float tlx = fmaf(lx, ax, bx), thx = fmaf(hx, ax, bx);
-      const float tly = fmaf(ly, ay, by), thy = fmaf(hy, ay, by);
-      const float tlz = fmaf(lz, az, bz), thz = fmaf(hz, az, bz);
-      const float tn = fmaxf(fmaxf(fminf(tlx, thx), fminf(tly, thy)), fminf(tlz, thz));
-      const float tf = fminf(fminf(fmaxf(tlx, thx), fmaxf(tly, thy)), fmaxf(tlz, thz)) * kFarSlack;
+      // byte k as a float: bits 0x4B0000bb are 2^23 + bb, so subtracting 2^23 is exact
+      const uint32_t sel = 0x7540u + (uint32_t)(k & 3);
+      const uint32_t meta = __byte_perm(k < 4 ? m0 : m1, 0u, 0x4440u + (uint32_t)(k & 3));
+      const float nx = __uint_as_float(__byte_perm(k < 4 ? nx0 : nx1, 0x4B000000u, sel)) - 8388608.0f;
+      const float fx = __uint_as_float(__byte_perm(k < 4 ? fx0 : fx1, 0x4B000000u, sel)) - 8388608.0f;
+      const float ny = __uint_as_float(__byte_perm(k < 4 ? ny0 : ny1, 0x4B000000u, sel)) - 8388608.0f;
+      const float fy = __uint_as_float(__byte_perm(k < 4 ? fy0 : fy1, 0x4B000000u, sel)) - 8388608.0f;
+      const float nz = __uint_as_float(__byte_perm(k < 4 ? nz0 : nz1, 0x4B000000u, sel)) - 8388608.0f;
+      const float fz = __uint_as_float(__byte_perm(k < 4 ? fz0 : fz1, 0x4B000000u, sel)) - 8388608.0f;
+      const float tn = fmaxf(fmaxf(fmaf(nx, ax, bx), fmaf(ny, ay, by)), fmaf(nz, az, bz));
+      const float tf = fminf(fminf(fmaf(fx, ax, bx), fmaf(fy, ay, by)), fmaf(fz, az, bz)) * kFarSlack;
       const bool hit = meta != 0u && tn <= tf && tf >= 0.0f && tn < h.t;
       key[k] = 0xFFFFFFFFu;
       if (hit) {
-        if (in_blas && !(meta & 0x80u)) leaf_mask |= 1u << k;
-        else key[k] = (f2u(fmaxf(tn, 0.0f)) & ~7u) | (uint32_t)k;
+        if (in_blas && !(meta & 0x80u)) {
+          leaf_mask |= 1u << k;
+        } else {
+          key[k] = (f2u(fmaxf(tn, 0.0f)) & ~7u) | (uint32_t)k;
+          ++n_push;
+        }
       }
     }
 
@@ -188,12 +199,21 @@ __device__ __forceinline__ uint32_t trace_ray(const DevScene& s, const V3 wo, co
     key[j] = max(key[i], key[j]);                    \
     key[i] = lo_;                                    \
   }
-    NB_CX(0, 2) NB_CX(1, 3) NB_CX(4, 6) NB_CX(5, 7)
-    NB_CX(0, 4) NB_CX(1, 5) NB_CX(2, 6) NB_CX(3, 7)
-    NB_CX(0, 1) NB_CX(2, 3) NB_CX(4, 5) NB_CX(6, 7)
-    NB_CX(2, 4) NB_CX(3, 5)
-    NB_CX(1, 4) NB_CX(3, 6)
-    NB_CX(1, 2) NB_CX(3, 4) NB_CX(5, 6)
+    if (n_push > 1) {
+      NB_CX(0, 2) NB_CX(1, 3) NB_CX(4, 6) NB_CX(5, 7)
+      NB_CX(0, 4) NB_CX(1, 5) NB_CX(2, 6) NB_CX(3, 7)
+      NB_CX(0, 1) NB_CX(2, 3) NB_CX(4, 5) NB_CX(6, 7)
+      NB_CX(2, 4) NB_CX(3, 5)
+      NB_CX(1, 4) NB_CX(3, 6)
+      NB_CX(1, 2) NB_CX(3, 4) NB_CX(5, 6)
+    } else if (n_push == 1) {  // move the single key to the front
+      uint32_t m = key[0];
+#pragma unroll
+      for (int k = 1; k < 8; ++k) m = min(m, key[k]);
+#pragma unroll
+      for (int k = 1; k < 8; ++k) key[k] = 0xFFFFFFFFu;
+      key[0] = m;
+    }
 #undef NB_CX
     // push far to near; the nearest inner child is visited next without a push
 #pragma unroll

@@ -511,6 +511,30 @@ struct Collapser {
   std::vector<uint32_t>* prim_order;   // new order -> reference primitive index
   uint32_t max_leaf;                   // primitives per leaf slot (3 triangles, 1 instance)
 
+  struct Span {
+    uint32_t first = 0xFFFFFFFFu, end = 0, count = 0;
+  };
+  mutable std::vector<Span> span;  // memo: primitive range and leaf count of a subtree
+
+  // [first, end) of the primitives below binary node n.  bvh.rs partitions in place, so a
+  // subtree covers a contiguous range (count == end - first); trees handed in through
+  // nb_scene_create_from_bvh are only trusted where that holds.
+  Span subtree_span(uint32_t n) const {
+    if (span.empty()) span.assign(ref.size(), Span{});
+    if (span[n].first != 0xFFFFFFFFu) return span[n];
+    const nb_bvh_node& b = ref[n];
+    Span r;
+    if (b.end > 0) {
+      r = Span{b.start, b.end, b.end - b.start};
+    } else {
+      Span l = subtree_span(b.start), h = subtree_span(b.start + 1);
+      r = Span{std::min(l.first, h.first), std::max(l.end, h.end), l.count + h.count};
+    }
+    span[n] = r;
+    return r;
+  }
+
+  // a binary node becomes an item; subtrees of at most max_leaf primitives become one leaf
   Item item_of(uint32_t n) const {
     const nb_bvh_node& b = ref[n];
     Item it{};
@@ -518,6 +542,14 @@ struct Collapser {
     it.node = n;
     it.start = b.start;
     it.count = b.end > 0 ? b.end - b.start : 0;
+    if (it.inner) {
+      const Span r = subtree_span(n);
+      if (r.count <= max_leaf && r.end - r.first == r.count) {
+        it.inner = false;
+        it.start = r.first;
+        it.count = r.count;
+      }
+    }
     for (int k = 0; k < 3; ++k) { it.mn[k] = b.min[k]; it.mx[k] = b.max[k]; }
     return it;
   }
