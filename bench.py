@@ -49,6 +49,9 @@ def parse():
     p.add_argument("--width", type=int, default=1920, help="smaller frames for profiling runs only")
     p.add_argument("--height", type=int, default=1080)
     p.add_argument("--batch-paths", type=int, default=0, help="paths per wavefront batch (0: library default)")
+    p.add_argument("--no-serving", action="store_true", help="skip the render-job serving report")
+    p.add_argument("--serving-loads", type=str, default="10:60,30:90,60:120",
+                   help="rate:jobs pairs of Poisson loads for the serving report")
     return p.parse_args()
 
 
@@ -146,6 +149,35 @@ def cpu_baseline(desc, sobol, seconds, threads):
                       f"(oracle scene build {build_s:.1f} s, not timed)"}, per_ray, osc
 
 
+def serving_report(args):
+    """Render-job serving (continuous batching): 8 resident instanced scenes of ~10K to ~5M
+    unique triangles, one shared 2048x1024 sky, seeded Poisson arrivals; resolution uniform
+    over {256^2, 512^2, 1024x768, 1920x1080}, spp uniform over {1, 4, 16, 64}, 8 bounces,
+    120 GB admission budget.  The mix costs ~17M paths per job on average, so the arrival
+    rates are given beside the measured saturation throughput."""
+    import nbounce_gb300 as nb
+    from nbounce_gb300 import scenes, server
+    scales = [1 / 512, 1 / 128, 1 / 64, 1 / 16, 1 / 8, 1 / 4, 1 / 2, 1.0]
+    descs = [scenes.instanced_scene(seed=0x5EED1 + 97 * k, scale=s, width=64, height=64, env_size=(16, 8))
+             for k, s in enumerate(scales)]
+    bufs = [nb.SceneBuffers.from_desc(d) for d in descs]
+    sky = nb.EnvMap(texels=scenes.sky_envmap(0x5EED9, 2048, 1024))
+    srv = server.RenderServer(hbm_budget_bytes=120 << 30, paths_per_wave=1 << 25)
+    slots = [srv.add_scene(b) for b in bufs]
+    env = srv.add_env(sky)
+    eye, target = (0.0, 14.0, 62.0), (0.0, -2.0, 0.0)
+    cams = [lambda w, h: scenes.camera_matrices(eye, target, w, h)] * len(descs)
+    server.run_load(srv, slots, env, cams, server.make_trace(8, 1000.0, len(descs), seed=1))  # warm-up
+    out = {"scenes_unique_triangles": [int(d.n_triangles_unique) for d in descs], "budget_gb": 120,
+           "paths_per_wave": 1 << 25, "loads": []}
+    for rate, n_jobs in args.serving_loads:
+        r = server.run_load(srv, slots, env, cams, server.make_trace(n_jobs, rate, len(descs), seed=int(rate)))
+        r["rate_jobs_per_s"] = rate
+        out["loads"].append({k: (round(v, 3) if isinstance(v, float) else v) for k, v in r.items()})
+    srv.close()
+    return out
+
+
 def run_ours(args):
     import torch
     import nbounce_gb300 as nb
@@ -240,6 +272,8 @@ def run_ours(args):
                                                                        "accumulate_ms")},
         "clocks": clocks.summary(),
     }
+    if not args.no_serving and world == 1:
+        line["serving"] = serving_report(args)
     peak, peak_kind = measured_peaks()
     sobol = nb.sobol_burley_table()
     if not args.no_cpu_baseline:
@@ -296,6 +330,7 @@ def run_reference(args):
 
 def main():
     args = parse()
+    args.serving_loads = [(float(a), int(b)) for a, b in (x.split(":") for x in args.serving_loads.split(","))]
     line = run_reference(args) if args.impl == "reference" else run_ours(args)
     if line is not None:
         print(json.dumps(line), flush=True)

@@ -260,6 +260,63 @@ int nb_scene_status(const nb_scene* scene, uint32_t* status, void* stream);
 int nb_trace_rays_host(const nb_scene* scene, const float* rays, size_t n, uint32_t flags, float* hits,
                        uint32_t* instances, void* stream);
 
+/* ---------------------------------------------------------------------------------------
+ * Render-job server (continuous batching).  No counterpart in the reference, which renders
+ * one progressive image per window: this serves many render requests against resident
+ * scenes.  A scheduler thread admits queued jobs while their images fit the HBM budget,
+ * packs samples of all admitted jobs into shared wavefronts (one segment of consecutive
+ * Sobol rows per job per wave, paths of several scenes in one trace launch), and keeps up to
+ * two waves in flight.  A job's image is bit-identical to rendering it alone with
+ * nb_pathtracer_render: every path depends only on its own job, pixel and sample, and each
+ * job's samples are accumulated in sample order.
+ * ------------------------------------------------------------------------------------- */
+typedef struct nb_server nb_server;
+
+typedef struct nb_job_desc {
+  uint32_t scene;               /* slot from nb_server_add_scene */
+  uint32_t env;                 /* slot from nb_server_add_env */
+  nb_camera camera;
+  uint32_t width, height;
+  uint32_t spp;                 /* samples: Sobol rows 1..spp of the server's table */
+  uint32_t bounces;
+  float contribution_factor;
+  uint32_t flags;               /* reserved, 0 */
+  float* host_out;              /* optional: width*height RGBA32F copied here when done */
+} nb_job_desc;
+
+typedef struct nb_job_info {
+  int status;                   /* NB_OK once finished, else the job's error */
+  uint32_t done;                /* 1 when finished (or failed) */
+  double submit_ms, admit_ms, finish_ms;  /* server clock (ms since nb_server_create) */
+} nb_job_info;
+
+typedef struct nb_server_stats {
+  uint64_t jobs_submitted, jobs_done, jobs_failed, waves;
+  uint64_t rays;                /* traversal queries of all waves so far */
+  double gpu_busy_ms;           /* sum of wave durations (CUDA events) */
+  uint64_t bytes_in_use, peak_bytes_in_use, budget_bytes;
+  uint32_t queued, active;
+} nb_server_stats;
+
+/* hbm_budget_bytes bounds the server's device memory (path buffers + job images);
+ * paths_per_wave sizes the shared path buffers (at least one image of the largest job). */
+int nb_server_create(uint64_t hbm_budget_bytes, uint32_t paths_per_wave, nb_server** out);
+/* Registers a resident scene / environment (the caller keeps them alive until destroy). */
+int nb_server_add_scene(nb_server* server, const nb_scene* scene, uint32_t* slot);
+int nb_server_add_env(nb_server* server, const nb_env* env, uint32_t* slot);
+/* Queues a job; thread-safe, returns at once.  NB_ERR_INVALID_ARG for bad slots or sizes,
+ * NB_ERR_OOM if the job can never fit the budget. */
+int nb_server_submit(nb_server* server, const nb_job_desc* job, uint64_t* job_id);
+/* Waits up to timeout_ms (< 0: forever) for a job; NB_ERR_TIMEOUT if it is not done yet. */
+int nb_server_wait(nb_server* server, uint64_t job_id, int timeout_ms, nb_job_info* info);
+/* Copies a finished job's image (when it was submitted without host_out) and frees it. */
+int nb_server_fetch(nb_server* server, uint64_t job_id, float* host_rgba);
+/* Forgets a finished job's record. */
+int nb_server_release(nb_server* server, uint64_t job_id);
+int nb_server_get_stats(nb_server* server, nb_server_stats* stats);
+/* Finishes the queued and active jobs, then stops the scheduler and frees its memory. */
+void nb_server_destroy(nb_server* server);
+
 #ifdef __cplusplus
 }
 #endif

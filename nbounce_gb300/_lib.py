@@ -61,6 +61,24 @@ class NbKernelTimes(C.Structure):
                 ("shade_launches", C.c_uint64), ("accumulate_launches", C.c_uint64)]
 
 
+class NbJobDesc(C.Structure):
+    _fields_ = [("scene", C.c_uint32), ("env", C.c_uint32), ("camera", NbCamera), ("width", C.c_uint32),
+                ("height", C.c_uint32), ("spp", C.c_uint32), ("bounces", C.c_uint32),
+                ("contribution_factor", C.c_float), ("flags", C.c_uint32), ("host_out", C.c_void_p)]
+
+
+class NbJobInfo(C.Structure):
+    _fields_ = [("status", C.c_int), ("done", C.c_uint32), ("submit_ms", C.c_double), ("admit_ms", C.c_double),
+                ("finish_ms", C.c_double)]
+
+
+class NbServerStats(C.Structure):
+    _fields_ = [("jobs_submitted", C.c_uint64), ("jobs_done", C.c_uint64), ("jobs_failed", C.c_uint64),
+                ("waves", C.c_uint64), ("rays", C.c_uint64), ("gpu_busy_ms", C.c_double),
+                ("bytes_in_use", C.c_uint64), ("peak_bytes_in_use", C.c_uint64), ("budget_bytes", C.c_uint64),
+                ("queued", C.c_uint32), ("active", C.c_uint32)]
+
+
 class NbError(RuntimeError):
     def __init__(self, status, message):
         super().__init__(f"{message} (status {status})")
@@ -111,6 +129,15 @@ def lib():
         "nb_pathtracer_kernel_times": ([vp, vp, i32, vp], i32),
         "nb_trace_rays": ([vp, vp, sz, u32, vp, vp, vp], i32),
         "nb_trace_rays_host": ([vp, vp, sz, u32, vp, vp, vp], i32),
+        "nb_server_create": ([u64, u32, vp], i32),
+        "nb_server_add_scene": ([vp, vp, vp], i32),
+        "nb_server_add_env": ([vp, vp, vp], i32),
+        "nb_server_submit": ([vp, vp, vp], i32),
+        "nb_server_wait": ([vp, u64, i32, vp], i32),
+        "nb_server_fetch": ([vp, u64, vp], i32),
+        "nb_server_release": ([vp, u64], i32),
+        "nb_server_get_stats": ([vp, vp], i32),
+        "nb_server_destroy": ([vp], None),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

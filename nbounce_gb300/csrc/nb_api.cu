@@ -9,6 +9,7 @@
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <memory>
 #include <new>
 #include <string>
 #include <tuple>
@@ -16,6 +17,7 @@
 
 #include "nb_internal.h"
 #include "nb_launch.h"
+#include "nb_runtime.h"
 
 namespace nb {
 
@@ -31,74 +33,9 @@ int fail(int status, const char* fmt, ...) {
   return status;
 }
 
-static int cuda_fail(cudaError_t e, const char* what) {
-  if (e == cudaErrorMemoryAllocation) return fail(NB_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
-  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
-    return fail(NB_ERR_NO_DEVICE, "%s: %s", what, cudaGetErrorString(e));
-  return fail(NB_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
-}
-
-#define NB_CUDA(call, what)                       \
-  do {                                            \
-    cudaError_t e_ = (call);                      \
-    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
-  } while (0)
-
-static int sm_count() {
-  int dev = 0, sms = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
-  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 1;
-  return sms > 0 ? sms : 1;
-}
-
-// A list of device allocations released together.
-struct DeviceArena {
-  std::vector<void*> ptrs;
-  size_t bytes = 0;
-  template <class T>
-  int upload(const std::vector<T>& v, const T** out) {
-    if (v.empty()) { *out = nullptr; return NB_OK; }
-    void* p = nullptr;
-    NB_CUDA(cudaMalloc(&p, v.size() * sizeof(T)), "cudaMalloc(scene)");
-    ptrs.push_back(p);
-    bytes += v.size() * sizeof(T);
-    NB_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy(scene)");
-    *out = (const T*)p;
-    return NB_OK;
-  }
-  int alloc(size_t n, void** out) {
-    void* p = nullptr;
-    NB_CUDA(cudaMalloc(&p, n), "cudaMalloc");
-    ptrs.push_back(p);
-    bytes += n;
-    *out = p;
-    return NB_OK;
-  }
-  void release() {
-    for (void* p : ptrs) cudaFree(p);
-    ptrs.clear();
-    bytes = 0;
-  }
-};
-
 }  // namespace nb
 
 using namespace nb;
-
-struct nb_scene {
-  HostScene host;
-  nbd::DevScene dev{};
-  DeviceArena arena;
-  uint32_t* d_fetch = nullptr;
-  uint32_t* d_status = nullptr;
-  int sms = 1;
-  bool uploaded = false;
-};
-
-struct nb_env {
-  nbd::DevEnv dev{};
-  DeviceArena arena;
-};
 
 struct nb_pathtracer {
   uint32_t width = 0, height = 0;
@@ -115,6 +52,7 @@ struct nb_pathtracer {
   uint32_t* d_status = nullptr;
   unsigned long long* d_rays = nullptr;
   PathBatch pb{};
+  std::unique_ptr<WaveTables> wt{new WaveTables()};  // kernel parameter tables (host copy)
   uint32_t capacity = 0;  // paths the work buffers hold
   uint32_t batch_paths = 1u << 27;
   int sms = 1;
@@ -494,8 +432,22 @@ static int render_samples(nb_pathtracer* pt, const nb_scene* scene, const nb_cam
   const uint32_t npix = pt->width * pt->height;
   if (npix == 0 || n_samples == 0) return NB_OK;
   uint32_t remaining = std::min(n_samples, pt->max_sample_count - pt->globals.sample);
-  CameraParams cam;
-  std::memcpy(cam.c2w, camera->clip_to_world, sizeof(cam.c2w));
+  // one job, one segment per batch
+  WaveTables& wt = *pt->wt;
+  wt.n_jobs = 1;
+  wt.n_scenes = 1;
+  wt.n_segs = 1;
+  wt.scenes[0] = scene->dev;
+  JobParams& jp = wt.jobs[0];
+  std::memcpy(jp.c2w, camera->clip_to_world, sizeof(jp.c2w));
+  jp.env = env->dev;
+  jp.out = (float4*)pt->d_out;
+  jp.scene = 0;
+  jp.width = pt->width;
+  jp.height = pt->height;
+  jp.npix = npix;
+  jp.bounces = pt->globals.bounces;
+  jp.cf = pt->globals.contribution_factor;
   while (remaining > 0) {
     uint32_t S = batch_samples(pt, remaining);
     int rc = ensure_capacity(pt, npix * S);
@@ -506,23 +458,17 @@ static int render_samples(nb_pathtracer* pt, const nb_scene* scene, const nb_cam
     pb.status = pt->d_status;
     pb.sobol = pt->d_sobol;
     pb.sobol_entries = pt->sobol_entries;
-    pb.n_paths = npix * S;
-    pb.npix = npix;
-    pb.width = pt->width;
-    pb.height = pt->height;
-    pb.first_sample = pt->globals.sample + 1;  // dispatch increments before use (pathtracer.rs:234)
+    // dispatch increments the sample counter before use (pathtracer.rs:234)
+    wt.segs[0] = Segment{0u, pt->globals.sample + 1, S, 0u, 0u};
+    wt.n_paths = npix * S;
+    wt.n_pix = npix;
     const uint32_t B = pt->globals.bounces;
-    const float cf = pt->globals.contribution_factor;
-    cudaError_t e = timed_launch(pt, kKindRaygen, st, [&] { return launch_raygen(pb, cam, pt->sms, st); });
+    cudaError_t e = timed_launch(pt, kKindRaygen, st, [&] { return launch_raygen(pb, wt, pt->sms, st); });
     for (uint32_t b = 0; b <= B && e == cudaSuccess; ++b) {
-      e = timed_launch(pt, kKindTrace, st,
-                       [&] { return launch_trace_wave(scene->dev, pb, b, pt->d_rays, pt->sms, st); });
-      if (e == cudaSuccess)
-        e = timed_launch(pt, kKindShade, st,
-                         [&] { return launch_shade(scene->dev, env->dev, pb, b, B, cf, pt->sms, st); });
+      e = timed_launch(pt, kKindTrace, st, [&] { return launch_trace_wave(pb, wt, true, b, pt->d_rays, pt->sms, st); });
+      if (e == cudaSuccess) e = timed_launch(pt, kKindShade, st, [&] { return launch_shade(pb, wt, b, pt->sms, st); });
     }
-    if (e == cudaSuccess)
-      e = timed_launch(pt, kKindAccumulate, st, [&] { return launch_accumulate(pb, S, pt->d_out, pt->sms, st); });
+    if (e == cudaSuccess) e = timed_launch(pt, kKindAccumulate, st, [&] { return launch_accumulate(pb, wt, pt->sms, st); });
     if (e != cudaSuccess) return cuda_fail(e, "path batch launch");
     pt->globals.sample += S;
     pt->globals.weight = 1.0f / (float)pt->globals.sample;

@@ -13,7 +13,9 @@
 //               choice, VNDF / cosine sampling, Russian roulette (pathtracing.wgsl:161-241);
 //               survivors are appended to the next bounce's queue with warp-aggregated atomics
 //   accumulate  running mean over the batch's samples in sample order (pathtracing.wgsl:258)
-// so traversal runs in a lean kernel and the path state lives in HBM.
+// so traversal runs in a lean kernel and the path state lives in HBM.  A wave can hold paths
+// of several jobs (render requests): tables of segments, jobs and scenes ride in the kernel
+// parameters and each path finds its job through its path id.
 //
 // The traversal finds the reference's closest hit: quantised boxes contain the reference
 // boxes, triangles are tested with the reference's Moller-Trumbore arithmetic, and a hit
@@ -30,9 +32,11 @@
 
 namespace nbd {
 
-using nb::CameraParams;
+using nb::JobParams;
 using nb::kMaxBounceSlots;
 using nb::PathBatch;
+using nb::Segment;
+using nb::WaveTables;
 
 constexpr int kStackSize = 64;
 constexpr uint32_t kIterationCap = 1u << 22;
@@ -265,6 +269,7 @@ __global__ void __launch_bounds__(128) k_trace_rays(DevScene s, const float4* __
   if (st) atomicOr(status, st);
 }
 
+
 // ------------------------------------------------------------------------------------------
 // wavefront path tracer
 // ------------------------------------------------------------------------------------------
@@ -272,12 +277,11 @@ __device__ __forceinline__ float4 sobol_read(const float4* table, uint32_t n_ent
   return idx < n_entries ? __ldg(table + idx) : make_float4(0.f, 0.f, 0.f, 0.f);  // robust buffer access
 }
 
-// generate_ray (pathtracing.wgsl:27-41)
+// generate_ray (pathtracing.wgsl:27-41); m is clip_to_world, column-major
 __device__ __forceinline__ void generate_ray(uint32_t x, uint32_t y, uint32_t W, uint32_t H, float rx, float ry,
-                                             const CameraParams& cam, V3* o, V3* d) {
+                                             const float* m, V3* o, V3* d) {
   float uvx = 2.0f * ((float)x + rx) / (float)W - 1.0f;
   float uvy = 2.0f * ((float)y + ry) / (float)H - 1.0f;
-  const float* m = cam.c2w;
   V3 pos = V3{m[12], m[13], m[14]} / m[15];
   float cx = -uvx, cy = -uvy, cz = -1.0f, cw = 1.0f;
   float wd[4];
@@ -287,30 +291,60 @@ __device__ __forceinline__ void generate_ray(uint32_t x, uint32_t y, uint32_t W,
   *d = pos - V3{wd[0], wd[1], wd[2]} / wd[3];
 }
 
-__global__ void __launch_bounds__(256) k_raygen(PathBatch pb, CameraParams cam) {
-  const uint32_t n = pb.n_paths;
+// index of the last segment whose begin (path or accumulate index) is <= p
+template <bool kByPixel>
+__device__ __forceinline__ uint32_t find_segment(const Segment* segs, uint32_t n, uint32_t p) {
+  uint32_t lo = 0, hi = n;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    const uint32_t b = kByPixel ? segs[mid].pix_begin : segs[mid].path_begin;
+    if (b <= p) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void stage_segments(Segment* dst, const WaveTables& wt) {
+  for (uint32_t i = threadIdx.x; i < wt.n_segs; i += blockDim.x) dst[i] = wt.segs[i];
+  __syncthreads();
+}
+
+__global__ void __launch_bounds__(256) k_raygen(PathBatch pb, const WaveTables wt) {
+  __shared__ Segment segs[nb::kMaxWaveSegments];
+  stage_segments(segs, wt);
+  const uint32_t n = wt.n_paths;
   if (blockIdx.x == 0 && threadIdx.x < kMaxBounceSlots) {
     pb.counts[threadIdx.x] = threadIdx.x == 0 ? n : 0u;
     pb.fetch[threadIdx.x] = 0u;
   }
   for (uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < n; p += gridDim.x * blockDim.x) {
-    uint32_t pix = p % pb.npix;
-    uint32_t sample = pb.first_sample + p / pb.npix;
-    uint32_t x = pix % pb.width, y = pix / pb.width;
-    float4 shift = hash4f(x, y);
-    float4 sb = sobol_read(pb.sobol, pb.sobol_entries, sample * kLdsStride);
-    float jx = fract(sb.x + shift.x), jy = fract(sb.y + shift.y);
+    const Segment sg = segs[find_segment<false>(segs, wt.n_segs, p)];
+    const JobParams& jp = wt.jobs[sg.job];
+    const uint32_t local = p - sg.path_begin;
+    const uint32_t pix = local % jp.npix;
+    const uint32_t sample = sg.first_sample + local / jp.npix;
+    const uint32_t x = pix % jp.width, y = pix / jp.width;
+    const float4 shift = hash4f(x, y);
+    const float4 sb = sobol_read(pb.sobol, pb.sobol_entries, sample * kLdsStride);
+    const float jx = fract(sb.x + shift.x), jy = fract(sb.y + shift.y);
     V3 o, d;
-    generate_ray(x, y, pb.width, pb.height, jx, jy, cam, &o, &d);
+    generate_ray(x, y, jp.width, jp.height, jx, jy, jp.c2w, &o, &d);
     pb.q_o[0][p] = make_float4(o.x, o.y, o.z, __uint_as_float(p));
-    pb.q_d[0][p] = make_float4(d.x, d.y, d.z, 0.0f);
+    pb.q_d[0][p] = make_float4(d.x, d.y, d.z, __uint_as_float(jp.scene));
     pb.q_t[0][p] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
     pb.radiance[p] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   }
 }
 
-__global__ void __launch_bounds__(128) k_trace_wave(DevScene s, PathBatch pb, uint32_t bounce,
+// kSingle: every ray of the wave uses wt.scenes[0]; else the scene index carried in q_d.w
+template <bool kSingle>
+__global__ void __launch_bounds__(128) k_trace_wave(PathBatch pb, const WaveTables wt, uint32_t bounce,
                                                     unsigned long long* __restrict__ ray_total) {
+  __shared__ DevScene scenes[kSingle ? 1 : nb::kMaxWaveScenes];
+  if (!kSingle) {
+    for (uint32_t i = threadIdx.x; i < wt.n_scenes; i += blockDim.x) scenes[i] = wt.scenes[i];
+    __syncthreads();
+  }
   const uint32_t n = pb.counts[bounce];
   const float4* __restrict__ qo = (bounce & 1) ? pb.q_o[1] : pb.q_o[0];
   const float4* __restrict__ qd = (bounce & 1) ? pb.q_d[1] : pb.q_d[0];
@@ -325,7 +359,7 @@ __global__ void __launch_bounds__(128) k_trace_wave(DevScene s, PathBatch pb, ui
     if (i < n) {
       const float4 o = qo[i], d = qd[i];
       Hit h;
-      st |= trace_ray<false>(s, xyz(o), xyz(d), h);
+      st |= trace_ray<false>(kSingle ? wt.scenes[0] : scenes[__float_as_uint(d.w)], xyz(o), xyz(d), h);
       pb.hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
       pb.hit_inst[i] = h.inst;
     }
@@ -420,8 +454,10 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool active) 
   return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
 }
 
-__global__ void __launch_bounds__(256) k_shade(DevScene s, DevEnv env, PathBatch pb, uint32_t bounce,
-                                               uint32_t bounces, float cf) {
+
+__global__ void __launch_bounds__(256) k_shade(PathBatch pb, const WaveTables wt, uint32_t bounce) {
+  __shared__ Segment segs[nb::kMaxWaveSegments];
+  stage_segments(segs, wt);
   const uint32_t n = pb.counts[bounce];
   const bool odd = (bounce & 1) != 0;
   const float4* __restrict__ in_o = odd ? pb.q_o[1] : pb.q_o[0];
@@ -437,95 +473,101 @@ __global__ void __launch_bounds__(256) k_shade(DevScene s, DevEnv env, PathBatch
     bool cont = false;
     float4 next_o = make_float4(0.f, 0.f, 0.f, 0.f), next_d = next_o, next_t = next_o;
     if (i < n) {
-      float4 O = in_o[i], D = in_d[i], Tq = in_t[i], H = pb.hits[i];
+      const float4 O = in_o[i], D = in_d[i], Tq = in_t[i], H = pb.hits[i];
       const uint32_t id = __float_as_uint(O.w);
+      const Segment sg = segs[find_segment<false>(segs, wt.n_segs, id)];
+      const JobParams& jp = wt.jobs[sg.job];
+      const DevScene& s = wt.scenes[jp.scene];
       V3 T = xyz(Tq);
-      V3 rdir = xyz(D);
+      const V3 rdir = xyz(D);
       if (H.x == kNoHit) {
-        V3 L = T * env_lookup(env, rdir);
+        const V3 L = T * env_lookup(jp.env, rdir);
         pb.radiance[id] = make_float4(L.x, L.y, L.z, 0.0f);
       } else {
         const uint32_t inst = pb.hit_inst[i];
         const float4* sh = s.inst_shade + 6 * (size_t)inst;
-        float4 c0 = ld4(sh), c1 = ld4(sh + 1), c2 = ld4(sh + 2);
-        float4 l0 = ld4(sh + 3), l1 = ld4(sh + 4), l2 = ld4(sh + 5);
-        V3 color{c0.w, c1.w, c2.w};
+        const float4 c0 = ld4(sh), c1 = ld4(sh + 1), c2 = ld4(sh + 2);
+        const float4 l0 = ld4(sh + 3), l1 = ld4(sh + 4), l2 = ld4(sh + 5);
+        const V3 color{c0.w, c1.w, c2.w};
         if (l2.w > 0.0f) {  // EMISSIVE (raytracing_sw.wgsl:168-170, pathtracing.wgsl:172-174)
-          V3 L = T * color;
+          const V3 L = T * color;
           pb.radiance[id] = make_float4(L.x, L.y, L.z, 0.0f);
         } else {
           // hit attributes (raytracing_sw.wgsl:146-158)
           const uint32_t tri = __float_as_uint(H.w);
           const uint32_t i0 = __ldg(s.tri_idx + 3 * (size_t)tri), i1 = __ldg(s.tri_idx + 3 * (size_t)tri + 1),
                          i2 = __ldg(s.tri_idx + 3 * (size_t)tri + 2);
-          float4 a0 = ld4(s.vattr + 2 * (size_t)i0), a1 = ld4(s.vattr + 2 * (size_t)i1), a2 = ld4(s.vattr + 2 * (size_t)i2);
-          float4 b0 = ld4(s.vattr + 2 * (size_t)i0 + 1), b1 = ld4(s.vattr + 2 * (size_t)i1 + 1),
-                 b2 = ld4(s.vattr + 2 * (size_t)i2 + 1);
+          const float4 a0 = ld4(s.vattr + 2 * (size_t)i0), a1 = ld4(s.vattr + 2 * (size_t)i1),
+                       a2 = ld4(s.vattr + 2 * (size_t)i2);
+          const float4 b0 = ld4(s.vattr + 2 * (size_t)i0 + 1), b1 = ld4(s.vattr + 2 * (size_t)i1 + 1),
+                       b2 = ld4(s.vattr + 2 * (size_t)i2 + 1);
           const float u = H.y, v = H.z;
           const float w0 = 1.0f - u - v;
-          V3 ln = xyz(a0) * w0 + xyz(a1) * u + xyz(a2) * v;
-          V3 lt = xyz(b0) * w0 + xyz(b1) * u + xyz(b2) * v;
-          V3 nrm{dot(xyz(c0), ln), dot(xyz(c1), ln), dot(xyz(c2), ln)};
-          V3 tng{dot(xyz(l0), lt), dot(xyz(l1), lt), dot(xyz(l2), lt)};
-          V3 pos = xyz(O) + H.x * rdir;
+          const V3 ln = xyz(a0) * w0 + xyz(a1) * u + xyz(a2) * v;
+          const V3 lt = xyz(b0) * w0 + xyz(b1) * u + xyz(b2) * v;
+          const V3 nrm{dot(xyz(c0), ln), dot(xyz(c1), ln), dot(xyz(c2), ln)};
+          const V3 tng{dot(xyz(l0), lt), dot(xyz(l1), lt), dot(xyz(l2), lt)};
+          const V3 pos = xyz(O) + H.x * rdir;
 
-          const uint32_t pix = id % pb.npix;
-          const uint32_t sample = pb.first_sample + id / pb.npix;
-          const float4 shift = hash4f(pix % pb.width, pix / pb.width);
+          const uint32_t local = id - sg.path_begin;
+          const uint32_t pix = local % jp.npix;
+          const uint32_t sample = sg.first_sample + local / jp.npix;
+          const float4 shift = hash4f(pix % jp.width, pix / jp.width);
           const float roughness = l0.w, metallic = l1.w;
           const float alpha = roughness * roughness;
           const float alpha2 = alpha * alpha;
-          V3 nn = normalize(nrm);
+          const V3 nn = normalize(nrm);
           const uint32_t sb = sample * kLdsStride + 1u + bounce * kLdsPerBounce;
           float4 s0 = sobol_read(pb.sobol, pb.sobol_entries, sb);
           float4 s1 = sobol_read(pb.sobol, pb.sobol_entries, sb + 1u);
           s0 = make_float4(fract(s0.x + shift.x), fract(s0.y + shift.y), fract(s0.z + shift.z), 0.0f);
           s1 = make_float4(0.0f, fract(s1.y + shift.y), fract(s1.z + shift.z), 0.0f);
-          V3 wo = normalize(-rdir);
-          float cosThetaO = dot(wo, nn);
+          const V3 wo = normalize(-rdir);
+          const float cosThetaO = dot(wo, nn);
           V3 wi;
-          V3 F0 = V3{0.04f, 0.04f, 0.04f} * (1.0f - metallic) + color * metallic;
-          float specular_weight = luminance(F_schlick(dot(wo, nn), F0));
-          float diffuse_weight = (1.0f - metallic) * luminance(color);
-          float p_specular = specular_weight / (specular_weight + diffuse_weight);
-          float p_diffuse = 1.0f - p_specular;
+          const V3 F0 = V3{0.04f, 0.04f, 0.04f} * (1.0f - metallic) + color * metallic;
+          const float specular_weight = luminance(F_schlick(dot(wo, nn), F0));
+          const float diffuse_weight = (1.0f - metallic) * luminance(color);
+          const float p_specular = specular_weight / (specular_weight + diffuse_weight);
+          const float p_diffuse = 1.0f - p_specular;
           if (s0.x < p_specular) {
-            V3 wm = sample_vndf_iso(s0.y, s0.z, wo, alpha, nn);
-            V3 ni = -wo;
+            const V3 wm = sample_vndf_iso(s0.y, s0.z, wo, alpha, nn);
+            const V3 ni = -wo;
             wi = ni - (2.0f * dot(wm, ni)) * wm;  // reflect(-wo, wm)
-            float cosThetaD = dot(wo, wm);
-            float cosThetaI = dot(wi, nn);
-            V3 F = F_schlick(cosThetaD, F0);
-            float LambdaL = lambda_tr(cosThetaI, alpha2);
-            float LambdaV = lambda_tr(cosThetaO, alpha2);
-            V3 spec = F * (1.0f + LambdaV) / (1.0f + LambdaL + LambdaV);
+            const float cosThetaD = dot(wo, wm);
+            const float cosThetaI = dot(wi, nn);
+            const V3 F = F_schlick(cosThetaD, F0);
+            const float LambdaL = lambda_tr(cosThetaI, alpha2);
+            const float LambdaV = lambda_tr(cosThetaO, alpha2);
+            const V3 spec = F * (1.0f + LambdaV) / (1.0f + LambdaL + LambdaV);
             T = T * (spec / p_specular);
           } else {
-            V3 nt = normalize(tng - dot(tng, nn) * nn);  // build_tbn (common.wgsl:55-59)
-            V3 bt = cross(nn, nt);
-            float phi = kTwoPi * s1.y;
-            float sinT = sqrtf(1.0f - s1.z);
-            float cosT = sqrtf(s1.z);
+            const V3 nt = normalize(tng - dot(tng, nn) * nn);  // build_tbn (common.wgsl:55-59)
+            const V3 bt = cross(nn, nt);
+            const float phi = kTwoPi * s1.y;
+            const float sinT = sqrtf(1.0f - s1.z);
+            const float cosT = sqrtf(s1.z);
             float sp, cp;
             nb_sincos(phi, &sp, &cp);
-            V3 ls{cp * sinT, sp * sinT, cosT};
+            const V3 ls{cp * sinT, sp * sinT, cosT};
             wi = nt * ls.x + bt * ls.y + nn * ls.z;
-            V3 wm = normalize(wi + wo);
-            float cosThetaD = dot(wi, wm);
-            float cosThetaI = dot(wi, nn);
-            float FD90 = 0.5f + 2.0f * alpha * pow2(cosThetaD);
-            float response = (1.0f + (FD90 - 1.0f) * pow5(1.0f - cosThetaI)) * (1.0f + (FD90 - 1.0f) * pow5(1.0f - cosThetaO));
-            V3 diffuse = (1.0f - metallic) * color * response;
+            const V3 wm = normalize(wi + wo);
+            const float cosThetaD = dot(wi, wm);
+            const float cosThetaI = dot(wi, nn);
+            const float FD90 = 0.5f + 2.0f * alpha * pow2(cosThetaD);
+            const float response =
+                (1.0f + (FD90 - 1.0f) * pow5(1.0f - cosThetaI)) * (1.0f + (FD90 - 1.0f) * pow5(1.0f - cosThetaO));
+            const V3 diffuse = (1.0f - metallic) * color * response;
             T = T * (diffuse / p_diffuse);
           }
           // Russian roulette (pathtracing.wgsl:225-236)
-          float p_continue = fminf(1.0f - pow8((float)bounce / (float)bounces), 1.0f);
-          p_continue = p_continue * fminf(luminance(T) * cf, 1.0f);
-          if (s0.z < p_continue && bounce < bounces) {
+          float p_continue = fminf(1.0f - pow8((float)bounce / (float)jp.bounces), 1.0f);
+          p_continue = p_continue * fminf(luminance(T) * jp.cf, 1.0f);
+          if (s0.z < p_continue && bounce < jp.bounces) {
             T = T / p_continue;
             cont = true;
             next_o = make_float4(pos.x, pos.y, pos.z, O.w);
-            next_d = make_float4(wi.x, wi.y, wi.z, 0.0f);
+            next_d = make_float4(wi.x, wi.y, wi.z, D.w);
             next_t = make_float4(T.x, T.y, T.z, 0.0f);
           }
         }
@@ -540,18 +582,24 @@ __global__ void __launch_bounds__(256) k_shade(DevScene s, DevEnv env, PathBatch
   }
 }
 
-// running mean in sample order: out = mix(out, L_k, 1/k) (pathtracing.wgsl:246-260)
-__global__ void __launch_bounds__(256) k_accumulate(PathBatch pb, float4* __restrict__ out, uint32_t n_samples) {
-  for (uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x; pix < pb.npix; pix += gridDim.x * blockDim.x) {
-    float4 c = out[pix];
-    for (uint32_t k = 0; k < n_samples; ++k) {
-      const float w = 1.0f / (float)(pb.first_sample + k);
-      const float4 L = pb.radiance[(size_t)k * pb.npix + pix];
+// running mean in sample order: out = mix(out, L_k, 1/k) (pathtracing.wgsl:246-260).  Each job
+// has at most one segment per wave, so every pixel has one writer.
+__global__ void __launch_bounds__(256) k_accumulate(PathBatch pb, const WaveTables wt) {
+  __shared__ Segment segs[nb::kMaxWaveSegments];
+  stage_segments(segs, wt);
+  for (uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < wt.n_pix; t += gridDim.x * blockDim.x) {
+    const Segment sg = segs[find_segment<true>(segs, wt.n_segs, t)];
+    const JobParams& jp = wt.jobs[sg.job];
+    const uint32_t pix = t - sg.pix_begin;
+    float4 c = jp.out[pix];
+    for (uint32_t k = 0; k < sg.n_samples; ++k) {
+      const float w = 1.0f / (float)(sg.first_sample + k);
+      const float4 L = pb.radiance[(size_t)sg.path_begin + (size_t)k * jp.npix + pix];
       c.x = c.x * (1.0f - w) + L.x * w;
       c.y = c.y * (1.0f - w) + L.y * w;
       c.z = c.z * (1.0f - w) + L.z * w;
     }
-    out[pix] = make_float4(c.x, c.y, c.z, 1.0f);
+    jp.out[pix] = make_float4(c.x, c.y, c.z, 1.0f);
   }
 }
 
@@ -575,38 +623,42 @@ cudaError_t launch_trace_rays(const nbd::DevScene& s, const float* rays, uint32_
   if (e != cudaSuccess) return e;
   if (n == 0) return cudaSuccess;
   if (any) {
-    int g = blocks_for((const void*)nbd::k_trace_rays<true>, 128, sms);
+    static const int g = blocks_for((const void*)nbd::k_trace_rays<true>, 128, sms);
     nbd::k_trace_rays<true><<<g, 128, 0, st>>>(s, (const float4*)rays, n, (float4*)hits, inst, fetch, status);
   } else {
-    int g = blocks_for((const void*)nbd::k_trace_rays<false>, 128, sms);
+    static const int g = blocks_for((const void*)nbd::k_trace_rays<false>, 128, sms);
     nbd::k_trace_rays<false><<<g, 128, 0, st>>>(s, (const float4*)rays, n, (float4*)hits, inst, fetch, status);
   }
   return cudaGetLastError();
 }
 
-cudaError_t launch_raygen(const PathBatch& pb, const CameraParams& cam, int sms, cudaStream_t st) {
-  int g = (int)std::min<uint64_t>((pb.n_paths + 255) / 256, (uint64_t)sms * 16);
-  nbd::k_raygen<<<g < 1 ? 1 : g, 256, 0, st>>>(pb, cam);
+cudaError_t launch_raygen(const PathBatch& pb, const WaveTables& wt, int sms, cudaStream_t st) {
+  int g = (int)std::min<uint64_t>((wt.n_paths + 255) / 256, (uint64_t)sms * 16);
+  nbd::k_raygen<<<g < 1 ? 1 : g, 256, 0, st>>>(pb, wt);
   return cudaGetLastError();
 }
 
-cudaError_t launch_trace_wave(const nbd::DevScene& s, const PathBatch& pb, uint32_t bounce,
+cudaError_t launch_trace_wave(const PathBatch& pb, const WaveTables& wt, bool single_scene, uint32_t bounce,
                               unsigned long long* ray_total, int sms, cudaStream_t st) {
-  static const int grid = blocks_for((const void*)nbd::k_trace_wave, 128, sms);
-  nbd::k_trace_wave<<<grid, 128, 0, st>>>(s, pb, bounce, ray_total);
+  if (single_scene) {
+    static const int g = blocks_for((const void*)nbd::k_trace_wave<true>, 128, sms);
+    nbd::k_trace_wave<true><<<g, 128, 0, st>>>(pb, wt, bounce, ray_total);
+  } else {
+    static const int g = blocks_for((const void*)nbd::k_trace_wave<false>, 128, sms);
+    nbd::k_trace_wave<false><<<g, 128, 0, st>>>(pb, wt, bounce, ray_total);
+  }
   return cudaGetLastError();
 }
 
-cudaError_t launch_shade(const nbd::DevScene& s, const nbd::DevEnv& env, const PathBatch& pb, uint32_t bounce,
-                         uint32_t bounces, float cf, int sms, cudaStream_t st) {
-  static const int grid = blocks_for((const void*)nbd::k_shade, 256, sms);
-  nbd::k_shade<<<grid, 256, 0, st>>>(s, env, pb, bounce, bounces, cf);
+cudaError_t launch_shade(const PathBatch& pb, const WaveTables& wt, uint32_t bounce, int sms, cudaStream_t st) {
+  static const int g = blocks_for((const void*)nbd::k_shade, 256, sms);
+  nbd::k_shade<<<g, 256, 0, st>>>(pb, wt, bounce);
   return cudaGetLastError();
 }
 
-cudaError_t launch_accumulate(const PathBatch& pb, uint32_t n_samples, float* out, int sms, cudaStream_t st) {
-  int g = (int)std::min<uint64_t>((pb.npix + 255) / 256, (uint64_t)sms * 16);
-  nbd::k_accumulate<<<g < 1 ? 1 : g, 256, 0, st>>>(pb, (float4*)out, n_samples);
+cudaError_t launch_accumulate(const PathBatch& pb, const WaveTables& wt, int sms, cudaStream_t st) {
+  int g = (int)std::min<uint64_t>((wt.n_pix + 255) / 256, (uint64_t)sms * 16);
+  nbd::k_accumulate<<<g < 1 ? 1 : g, 256, 0, st>>>(pb, wt);
   return cudaGetLastError();
 }
 

@@ -1,4 +1,9 @@
-// Kernel parameter blocks and launcher declarations (nb_kernels.cu <-> nb_api.cu).
+// Kernel parameter blocks and launcher declarations (nb_kernels.cu <-> nb_api.cu, nb_server.cu).
+//
+// A wave is one wavefront of paths: raygen, then trace + shade per bounce, then accumulate.
+// Its paths come from segments; a segment is a run of consecutive samples of one job (one
+// render request: scene, camera, environment, image).  The single-image Pathtracer runs
+// waves of one segment; the server packs segments of many jobs into one wave.
 #pragma once
 
 #include <cstdint>
@@ -9,16 +14,42 @@
 namespace nb {
 
 constexpr uint32_t kMaxBounceSlots = 64;  // per-bounce queue counters (bounces <= 62)
+constexpr uint32_t kMaxWaveJobs = 32;     // jobs per wave
+constexpr uint32_t kMaxWaveSegments = 64; // segments per wave
+constexpr uint32_t kMaxWaveScenes = 16;   // distinct scenes per wave
 
-struct CameraParams {
-  float c2w[16];  // clip_to_world, column-major
+struct JobParams {
+  float c2w[16];        // clip_to_world, column-major
+  nbd::DevEnv env;
+  float4* out;          // RGBA32F image, width * height
+  uint32_t scene;       // index into WaveTables::scenes
+  uint32_t width, height, npix;
+  uint32_t bounces;
+  float cf;             // contribution_factor
+  uint32_t pad[2];
 };
 
-// Device work buffers of one batch of paths (n_paths = npix * samples of the batch).
-// Paths are numbered p = k * npix + pixel for the batch's k-th sample.
+struct Segment {
+  uint32_t job;           // index into WaveTables::jobs
+  uint32_t first_sample;  // 1-based Sobol row of the segment's first sample
+  uint32_t n_samples;
+  uint32_t path_begin;    // first path id of the segment in the wave
+  uint32_t pix_begin;     // first accumulate thread of the segment
+};
+
+// Passed by value to the wave kernels (well under the 32 KB parameter limit).
+struct WaveTables {
+  uint32_t n_segs, n_jobs, n_scenes, n_paths, n_pix;
+  uint32_t pad[3];
+  Segment segs[kMaxWaveSegments];
+  JobParams jobs[kMaxWaveJobs];
+  nbd::DevScene scenes[kMaxWaveScenes];
+};
+
+// Device work buffers of a wave.  Path p is sample p / npix, pixel p % npix of its segment.
 struct PathBatch {
   float4* q_o[2];       // ray origin, .w = path id (bits); double-buffered queues
-  float4* q_d[2];       // ray direction
+  float4* q_d[2];       // ray direction, .w = scene index (bits)
   float4* q_t[2];       // throughput
   float4* hits;         // t, u, v, triangle (bits)
   uint32_t* hit_inst;   // TLAS-permuted instance of the hit
@@ -28,20 +59,16 @@ struct PathBatch {
   uint32_t* status;     // device status word
   const float4* sobol;  // Sobol-Burley table, kLdsStride vec4 per sample row
   uint32_t sobol_entries;
-  uint32_t n_paths;
-  uint32_t npix, width, height;
-  uint32_t first_sample;  // 1-based Sobol row of the batch's first sample
 };
 
 cudaError_t launch_trace_rays(const nbd::DevScene& s, const float* rays, uint32_t n, bool any, float* hits,
                               uint32_t* inst, uint32_t* fetch, uint32_t* status, int sms, cudaStream_t st);
 
-// one batch = raygen, then trace + shade per bounce 0..bounces, then accumulate
-cudaError_t launch_raygen(const PathBatch& pb, const CameraParams& cam, int sms, cudaStream_t st);
-cudaError_t launch_trace_wave(const nbd::DevScene& s, const PathBatch& pb, uint32_t bounce,
+cudaError_t launch_raygen(const PathBatch& pb, const WaveTables& wt, int sms, cudaStream_t st);
+// single_scene: all paths use wt.scenes[0] (passed by value); otherwise each ray's scene index
+cudaError_t launch_trace_wave(const PathBatch& pb, const WaveTables& wt, bool single_scene, uint32_t bounce,
                               unsigned long long* ray_total, int sms, cudaStream_t st);
-cudaError_t launch_shade(const nbd::DevScene& s, const nbd::DevEnv& env, const PathBatch& pb, uint32_t bounce,
-                         uint32_t bounces, float cf, int sms, cudaStream_t st);
-cudaError_t launch_accumulate(const PathBatch& pb, uint32_t n_samples, float* out, int sms, cudaStream_t st);
+cudaError_t launch_shade(const PathBatch& pb, const WaveTables& wt, uint32_t bounce, int sms, cudaStream_t st);
+cudaError_t launch_accumulate(const PathBatch& pb, const WaveTables& wt, int sms, cudaStream_t st);
 
 }  // namespace nb

@@ -1,0 +1,80 @@
+// Host runtime pieces shared by the C ABI (nb_api.cu) and the job server (nb_server.cu):
+// CUDA error mapping, the device allocation arena and the scene / environment handles.
+#pragma once
+
+#include <cstdio>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "nb_internal.h"
+#include "nb_launch.h"
+
+namespace nb {
+
+inline int cuda_fail(cudaError_t e, const char* what) {
+  if (e == cudaErrorMemoryAllocation) return fail(NB_ERR_OOM, "%s: %s", what, cudaGetErrorString(e));
+  if (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver)
+    return fail(NB_ERR_NO_DEVICE, "%s: %s", what, cudaGetErrorString(e));
+  return fail(NB_ERR_CUDA, "%s: %s", what, cudaGetErrorString(e));
+}
+
+#define NB_CUDA(call, what)                       \
+  do {                                            \
+    cudaError_t e_ = (call);                      \
+    if (e_ != cudaSuccess) return cuda_fail(e_, what); \
+  } while (0)
+
+inline int sm_count() {
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return 1;
+  if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) return 1;
+  return sms > 0 ? sms : 1;
+}
+
+// A list of device allocations released together.
+struct DeviceArena {
+  std::vector<void*> ptrs;
+  size_t bytes = 0;
+  template <class T>
+  int upload(const std::vector<T>& v, const T** out) {
+    if (v.empty()) { *out = nullptr; return NB_OK; }
+    void* p = nullptr;
+    NB_CUDA(cudaMalloc(&p, v.size() * sizeof(T)), "cudaMalloc(scene)");
+    ptrs.push_back(p);
+    bytes += v.size() * sizeof(T);
+    NB_CUDA(cudaMemcpy(p, v.data(), v.size() * sizeof(T), cudaMemcpyHostToDevice), "cudaMemcpy(scene)");
+    *out = (const T*)p;
+    return NB_OK;
+  }
+  int alloc(size_t n, void** out) {
+    void* p = nullptr;
+    NB_CUDA(cudaMalloc(&p, n), "cudaMalloc");
+    ptrs.push_back(p);
+    bytes += n;
+    *out = p;
+    return NB_OK;
+  }
+  void release() {
+    for (void* p : ptrs) cudaFree(p);
+    ptrs.clear();
+    bytes = 0;
+  }
+};
+
+}  // namespace nb
+
+struct nb_scene {
+  nb::HostScene host;
+  nbd::DevScene dev{};
+  nb::DeviceArena arena;
+  uint32_t* d_fetch = nullptr;
+  uint32_t* d_status = nullptr;
+  int sms = 1;
+  bool uploaded = false;
+};
+
+struct nb_env {
+  nbd::DevEnv dev{};
+  nb::DeviceArena arena;
+};

@@ -1,0 +1,110 @@
+"""Render-job server: continuous batching on the GPU.
+
+Each job's image must be bit-identical to rendering the same job alone with the
+Pathtracer (every path depends only on its job, pixel and sample; samples reach the image in
+order), whatever it was batched with; admission must respect the HBM budget.
+"""
+import numpy as np
+import pytest
+
+import nbounce_gb300 as nb
+from nbounce_gb300 import scenes
+from nbounce_gb300.server import RenderServer
+
+pytestmark = pytest.mark.gpu
+
+PATH_BYTES = 8 * 16 + 4  # per path of the server's buffers
+
+
+def fixed_bytes(paths):
+    return paths * PATH_BYTES + 1024 * 17 * 16 + 2 * 64 * 4 + 16 + 8
+
+
+@pytest.fixture(scope="module")
+def world():
+    sph = scenes.spheres_scene(width=48, height=32, spp=3, bounces=6)
+    ins = scenes.instanced_scene(n_instances=64, width=40, height=24, spp=2, bounces=8, env_size=(64, 32),
+                                 scale=1 / 128)
+    s0 = nb.SceneBuffers.from_desc(sph)
+    s1 = nb.SceneBuffers.from_desc(ins)
+    e0 = nb.EnvMap(sph.env_color)
+    e1 = nb.EnvMap(texels=ins.env_texels)
+    return dict(descs=(sph, ins), scenes=(s0, s1), envs=(e0, e1))
+
+
+def alone(world, k, w, h, spp, bounces):
+    desc = world["descs"][k]
+    w2c, c2w = scenes.camera_matrices(*CAMS[k], w, h)
+    pt = nb.Pathtracer(w, h, nb.Globals(bounces=bounces))
+    pt.render(world["scenes"][k], nb.camera_struct(w2c, c2w), world["envs"][k], spp)
+    return pt.download()
+
+
+CAMS = {0: ((0.0, 6.0, 34.0), (0.0, -1.0, 0.0)), 1: ((0.0, 14.0, 62.0), (0.0, -2.0, 0.0))}
+JOBS = [(0, 48, 32, 3, 6), (1, 40, 24, 2, 8), (0, 64, 64, 5, 4), (1, 32, 32, 1, 8), (0, 16, 48, 7, 6),
+        (1, 80, 40, 3, 2)]
+
+
+def submit_all(srv, slots, env_slots, outs):
+    ids = []
+    for (k, w, h, spp, b), out in zip(JOBS, outs):
+        w2c, c2w = scenes.camera_matrices(*CAMS[k], w, h)
+        ids.append(srv.submit(slots[k], env_slots[k], w2c, c2w, w, h, spp, b, out=out))
+    return ids
+
+
+def test_mixed_jobs_equal_jobs_rendered_alone(world):
+    paths = 1 << 14  # small waves: every job is split over several waves and shares them
+    srv = RenderServer(hbm_budget_bytes=1 << 30, paths_per_wave=paths)
+    slots = [srv.add_scene(s) for s in world["scenes"]]
+    env_slots = [srv.add_env(e) for e in world["envs"]]
+    outs = [np.full((h, w, 4), np.nan, np.float32) for (_, w, h, _, _) in JOBS]
+    ids = submit_all(srv, slots, env_slots, outs)
+    infos = [srv.wait(j, timeout_ms=120000) for j in ids]
+    assert all(i["done"] == 1 and i["status"] == 0 for i in infos)
+    st = srv.stats()
+    assert st["jobs_done"] == len(JOBS) and st["waves"] > 1
+    for (k, w, h, spp, b), out in zip(JOBS, outs):
+        ref = alone(world, k, w, h, spp, b)
+        assert np.array_equal(out, ref), (k, w, h, spp, b)
+    srv.close()
+
+
+def test_budget_limits_admission_and_all_jobs_finish(world):
+    paths = 1 << 14
+    biggest = max(w * h for (_, w, h, _, _) in JOBS) * 16
+    budget = fixed_bytes(paths) + 2 * biggest
+    srv = RenderServer(hbm_budget_bytes=budget, paths_per_wave=paths)
+    slots = [srv.add_scene(s) for s in world["scenes"]]
+    env_slots = [srv.add_env(e) for e in world["envs"]]
+    outs = [np.zeros((h, w, 4), np.float32) for (_, w, h, _, _) in JOBS]
+    ids = submit_all(srv, slots, env_slots, outs)
+    infos = [srv.wait(j, timeout_ms=120000) for j in ids]
+    assert all(i["done"] == 1 and i["status"] == 0 for i in infos)
+    st = srv.stats()
+    assert st["peak_bytes_in_use"] <= budget
+    assert all(np.isfinite(o).all() and (o[..., 3] == 1.0).all() for o in outs)
+    srv.close()
+
+
+def test_invalid_jobs_are_rejected(world):
+    paths = 1 << 12
+    srv = RenderServer(hbm_budget_bytes=fixed_bytes(paths) + 32 * 32 * 16, paths_per_wave=paths)
+    slot = srv.add_scene(world["scenes"][0])
+    env = srv.add_env(world["envs"][0])
+    w2c, c2w = scenes.camera_matrices(*CAMS[0], 32, 32)
+    with pytest.raises(nb.NbError) as e:
+        srv.submit(slot + 5, env, w2c, c2w, 32, 32, 1)
+    assert e.value.status == 1
+    with pytest.raises(nb.NbError) as e:  # larger than one wave's paths
+        srv.submit(slot, env, w2c, c2w, 128, 64, 1)
+    assert e.value.status == 1
+    with pytest.raises(nb.NbError) as e:  # fits one wave (2304 <= 4096 paths), not the budget
+        srv.submit(slot, env, w2c, c2w, 48, 48, 1)
+    assert e.value.status == 2
+    job = srv.submit(slot, env, w2c, c2w, 32, 32, 2)
+    info = srv.wait(job, timeout_ms=60000)
+    assert info["done"] == 1
+    img = srv.fetch(job, 32, 32)
+    assert np.array_equal(img, alone(world, 0, 32, 32, 2, 8))
+    srv.close()
