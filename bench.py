@@ -33,6 +33,10 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 METRIC = "Mrays/s (primary + extension rays), 1920x1080 64spp 8 bounces"
+# DRAM bytes (read + write) per traversal query of k_trace_wave, from one ncu capture of the
+# same scene at 480x270, 4 spp (bounce-0 launch: 518,400 rays, 99.5 MB read + 9.0 MB
+# written); the roofline scales it to a full launch by the launch's rays
+TRACE_DRAM_BYTES_PER_RAY = 209.4
 UNIT = "Mrays/s"
 WORKLOAD = "instanced 16 meshes / 1024 instances, 1920x1080, 64 spp, 8 bounces, equirect sky"
 
@@ -147,6 +151,37 @@ def cpu_baseline(desc, sobol, seconds, threads):
     return {"value": rays / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
             "sample": f"centred {w}x{h} crop of the 1920x1080 frame, {spp} spp, {rays} rays in {dt:.1f} s "
                       f"(oracle scene build {build_s:.1f} s, not timed)"}, per_ray, osc
+
+
+def rel_mse(img, ref):
+    """mean over pixels and channels of (x - ref)^2 / (ref^2 + 1e-2)"""
+    x = img[..., :3].astype(np.float64)
+    r = ref[..., :3].astype(np.float64)
+    return float(np.mean((x - r) ** 2 / (r * r + 1e-2)))
+
+
+def quality_report(args, ref_spp=16384, width=480, height=270):
+    """relMSE of the benchmark frame's 64-spp estimate against a 16,384-spp render of the same
+    camera and scene (FP32, this GPU), at 480x270 so the reference takes seconds."""
+    import nbounce_gb300 as nb
+    from nbounce_gb300 import scenes
+    desc = scenes.instanced_scene(spp=args.spp, width=width, height=height)
+    scene = nb.SceneBuffers.from_desc(desc)
+    env = nb.EnvMap(texels=desc.env_texels)
+    cam = nb.camera_struct(desc.world_to_clip, desc.clip_to_world)
+    table = nb.sobol_burley_table(ref_spp, 17)
+    pt = nb.Pathtracer(width, height, nb.Globals(bounces=desc.bounces), sobol_table=table)
+    t = time.perf_counter()
+    pt.render(scene, cam, env, ref_spp)
+    ref = pt.download()
+    ref_s = time.perf_counter() - t
+    out = {"resolution": [width, height], "reference_spp": ref_spp, "reference_s": round(ref_s, 2),
+           "reference": "FP32 GPU render, same camera/scene, Sobol rows 1..16384"}
+    for spp in (16, 64, 256):
+        pt.invalidate()
+        pt.render(scene, cam, env, spp)
+        out[f"relmse_{spp}spp"] = round(rel_mse(pt.download(), ref), 6)
+    return out
 
 
 def serving_report(args):
@@ -273,6 +308,7 @@ def run_ours(args):
         "clocks": clocks.summary(),
     }
     if not args.no_serving and world == 1:
+        line["quality"] = quality_report(args)
         line["serving"] = serving_report(args)
     peak, peak_kind = measured_peaks()
     sobol = nb.sobol_burley_table()
@@ -286,7 +322,9 @@ def run_ours(args):
         rays_per_launch = rays_per_step * args.steps / trace_launches
         achieved = bytes_per_ray * rays_per_launch / (avg_launch_ms / 1e3) / 1e9
         line["roofline"] = {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
-                            "frac": round(achieved / peak, 4), "traffic": None,
+                            "frac": round(achieved / peak, 4),
+                            "traffic": round(TRACE_DRAM_BYTES_PER_RAY * rays_per_launch),
+                            "traffic_note": "ncu dram bytes per ray of the 480x270 capture x rays per launch",
                             "kernel": "k_trace_wave", "peak_kind": f"{peak_kind} hbm_gbs (burst copy)",
                             "bytes_per_ray": round(bytes_per_ray, 1),
                             "work_per_ray": {"n_aabb": round(n_aabb, 2), "n_tri": round(n_tri, 2),
