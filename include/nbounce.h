@@ -255,6 +255,20 @@ int nb_trace_rays(const nb_scene* scene, const float* rays, size_t n, uint32_t f
 /* Synchronises stream and returns NB_ERR_STACK_OVERFLOW / NB_ERR_TIMEOUT if the last
  * traversal query on this scene raised the corresponding device status bit. */
 int nb_scene_status(const nb_scene* scene, uint32_t* status, void* stream);
+/* Renders samples first_sample .. first_sample + n_samples - 1 (1-based Sobol rows of the
+ * library's 1024-row table) into the caller's device RGBA32F image `out_rgba` (width * height,
+ * running mean as nb_pathtracer_dispatch keeps it) without allocating anything: for callers
+ * that cannot allocate device memory while they render (an engine that owns all GPU memory
+ * through its own allocator, a real-time loop whose footprint must stay fixed).  All scratch
+ * lives in one static device array of 34.9 MB reserved per GPU at library load; images above
+ * 262,144 pixels are rejected with NB_ERR_INVALID_ARG.  The first call on a device looks up
+ * that array and uploads the Sobol table - make it before any stream capture.  Calls share
+ * the array (it keeps the last call's contents); calls that overlap on the GPU race.
+ * Synchronises stream.  No counterpart in the reference. */
+int nb_render_static(const nb_scene* scene, const nb_env* env, const nb_camera* camera, uint32_t width,
+                     uint32_t height, uint32_t first_sample, uint32_t n_samples, uint32_t bounces,
+                     float contribution_factor, float* out_rgba, void* stream);
+
 /* Same query with host buffers: copies rays in and hits out inside the call and checks the
  * status word. */
 int nb_trace_rays_host(const nb_scene* scene, const float* rays, size_t n, uint32_t flags, float* hits,

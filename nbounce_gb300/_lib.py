@@ -129,6 +129,7 @@ def lib():
         "nb_pathtracer_kernel_times": ([vp, vp, i32, vp], i32),
         "nb_trace_rays": ([vp, vp, sz, u32, vp, vp, vp], i32),
         "nb_trace_rays_host": ([vp, vp, sz, u32, vp, vp, vp], i32),
+        "nb_render_static": ([vp, vp, vp, u32, u32, u32, u32, u32, C.c_float, vp, vp], i32),
         "nb_server_create": ([u64, u32, vp], i32),
         "nb_server_add_scene": ([vp, vp, vp], i32),
         "nb_server_add_env": ([vp, vp, vp], i32),
