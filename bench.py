@@ -13,6 +13,11 @@ same 132.7M paths.  Mrays/s counts traversal queries (primary + extension rays).
   e2e    the same frames through the C ABI with host buffers: the camera struct goes in and
          the 33 MB RGBA32F image comes back to pinned host memory inside every step.
 
+The line also carries `quality` (relMSE of 16/64/256 spp against a 16,384-spp render),
+`serving` (render-job server p50/p99 under Poisson loads) and `cache` (the learned radiance
+cache: online training along a seeded camera spline, then relMSE and frame time of cache
+mode against plain 16/64 spp at the last camera, with the MLP kernels' tensor-core rate).
+
 --impl reference times the CPU restatement of the reference pass (oracle/, all host
 threads) on crops of the same frame.  --gpus N runs N independent replicas (one frame each,
 weak scaling); there is no data-path collective.
@@ -56,6 +61,9 @@ def parse():
     p.add_argument("--no-serving", action="store_true", help="skip the render-job serving report")
     p.add_argument("--serving-loads", type=str, default="10:60,30:90,60:120",
                    help="rate:jobs pairs of Poisson loads for the serving report")
+    p.add_argument("--no-cache", action="store_true", help="skip the radiance-cache report")
+    p.add_argument("--cache-frames", type=int, default=300, help="1-spp frames of online training on the camera path")
+    p.add_argument("--cache-ref-spp", type=int, default=16384, help="samples of the cache report's reference image")
     return p.parse_args()
 
 
@@ -111,13 +119,17 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.rows)}
 
 
-def measured_peaks():
+def measured_peaks_all():
     try:
         with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
-            p = json.load(f)
-        return float(p["hbm_gbs"]), "measured"
-    except (OSError, KeyError, ValueError):
-        return 6800.0, "fallback"
+            return json.load(f)
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "fallback": True}
+
+
+def measured_peaks():
+    p = measured_peaks_all()
+    return float(p.get("hbm_gbs", 6800.0)), ("fallback" if p.get("fallback") else "measured")
 
 
 def build_workload(args):
@@ -210,6 +222,107 @@ def serving_report(args):
         r["rate_jobs_per_s"] = rate
         out["loads"].append({k: (round(v, 3) if isinstance(v, float) else v) for k, v in r.items()})
     srv.close()
+    return out
+
+
+# Algorithmic FLOPs of the radiance-cache MLP (64 -> 5 x 64 -> 3): a lookup is 5 * 64 * 64 +
+# 3 * 64 = 20,672 multiply-adds; a training record adds the backward pass, 4 * 4096 + 3 * 64 =
+# 16,576 for the hidden-layer gradients and 20,672 for the weight gradients.
+MLP_FLOP_PER_QUERY = 2 * 20672
+MLP_FLOP_PER_RECORD = 2 * (20672 + 16576 + 20672)
+
+
+def cache_report(args, desc, scene, env, stream):
+    """Learned radiance cache on the benchmark scene at the benchmark resolution: the cache
+    trains online for args.cache_frames one-sample frames while the camera moves along a
+    seeded spline (scenes.camera_path), then the last camera's frame is rendered with the
+    cache at 1, 4 and 16 spp and without it at 16 and 64 spp.  Every image is scored by
+    relMSE against an args.cache_ref_spp-sample plain render of that camera; frame times are
+    CUDA-event times of whole frames (render call: trace, shade, cache lookups, training,
+    accumulate).  Modes: "primary" ends every path at its primary hit (spread < 0), "spread"
+    uses the spread rule with c = 0.01."""
+    import torch
+    import nbounce_gb300 as nb
+    from nbounce_gb300 import scenes
+    W, H = desc.width, desc.height
+    sh = stream.cuda_stream
+    path = scenes.camera_path(args.cache_frames)
+    cams = [nb.camera_struct(*scenes.camera_matrices(e, t, W, H)) for e, t in path]
+    last = cams[-1]
+
+    def frame(pt, cam, spp):
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        pt.invalidate()
+        a.record(stream)
+        pt.render(scene, cam, env, spp, stream=sh)
+        b.record(stream)
+        b.synchronize()
+        return a.elapsed_time(b)
+
+    ref_pt = nb.Pathtracer(W, H, nb.Globals(bounces=desc.bounces), sobol_table=nb.sobol_burley_table(args.cache_ref_spp, 17))
+    t = time.perf_counter()
+    ref_pt.render(scene, last, env, args.cache_ref_spp, stream=sh)
+    ref = ref_pt.download(stream=sh)
+    ref_s = time.perf_counter() - t
+    ref_pt.close()
+    out = {"resolution": [W, H], "frames": args.cache_frames, "camera": "scenes.camera_path(seed 0x5EEDC), last frame",
+           "reference": f"plain FP32 GPU render, {args.cache_ref_spp} spp, {ref_s:.1f} s", "plain": {}, "modes": {}}
+    plain = nb.Pathtracer(W, H, nb.Globals(bounces=desc.bounces))
+    for spp in (16, 64):
+        frame(plain, last, spp)
+        ms = frame(plain, last, spp)
+        out["plain"][f"{spp}spp"] = {"relmse": round(rel_mse(plain.download(stream=sh), ref), 5), "ms": round(ms, 2)}
+    plain.close()
+    peak = measured_peaks_all().get("bf16_tflops")
+    for name, cfg in (("primary", dict(spread=-1.0)), ("spread", dict(spread=0.01))):
+        cache = nb.RadianceCache(seed=0x5EEDC, **cfg)
+        pt = nb.Pathtracer(W, H, nb.Globals(bounces=desc.bounces))
+        pt.set_cache(cache)
+        # training along the path; the last `timed` frames also record per-kernel times and
+        # cache counters (steady state: the training-path density has adapted to the budget)
+        timed = min(20, len(cams))
+        train_ms, queries, records = [], 0, 0
+        for k, cam in enumerate(cams):
+            if k == len(cams) - timed:
+                pt.enable_timing(True)
+                pt.kernel_times(reset=True, stream=sh)
+            train_ms.append(frame(pt, cam, 1))
+            if k >= len(cams) - timed:
+                st = cache.stats(stream=sh)
+                queries += st["queries"]
+                records += st["records_used"]
+        kt = pt.kernel_times(reset=True, stream=sh)
+        pt.enable_timing(False)
+        m = {"config": cache.config, "train_frame_ms_median": round(statistics.median(train_ms), 3),
+             "kernel_ms_per_frame": {k: round(kt[k] / timed, 3) for k in ("raygen_ms", "trace_ms", "shade_ms",
+                                                                          "cache_infer_ms", "cache_train_ms",
+                                                                          "accumulate_ms")},
+             "per_frame": {"queries": queries // timed, "records_used": records // timed,
+                           "stride": st["stride"], "loss": round(st["loss"], 4)}}
+        for spp in (1, 4, 16):
+            ms = frame(pt, last, spp)
+            m[f"{spp}spp"] = {"relmse": round(rel_mse(pt.download(stream=sh), ref), 5), "ms": round(ms, 2)}
+        infer_tf = queries * MLP_FLOP_PER_QUERY / (kt["cache_infer_ms"] / 1e3) / 1e12
+        train_tf = records * MLP_FLOP_PER_RECORD / (kt["cache_train_ms"] / 1e3) / 1e12
+        m["mlp_roofline"] = {"bound": "tensor", "unit": "TFLOP/s", "peak": peak,
+                             "infer_achieved": round(infer_tf, 1), "infer_frac": round(infer_tf / peak, 4) if peak else None,
+                             "train_achieved": round(train_tf, 2), "train_frac": round(train_tf / peak, 5) if peak else None,
+                             "note": "algorithmic FLOPs (41,344 per lookup, 115,840 per training record) over the "
+                                     "timed cache_infer / cache_train launches of the last 20 training frames "
+                                     "(train includes record gathering and the Adam launches)"}
+        out["modes"][name] = m
+        pt.close()
+        cache.close()
+    p64 = out["plain"]["64spp"]
+    best = None
+    for name, m in out["modes"].items():
+        for spp in (1, 4, 16):
+            r = m[f"{spp}spp"]
+            if r["relmse"] <= p64["relmse"] and (best is None or r["ms"] < best[2]):
+                best = (name, spp, r["ms"], r["relmse"])
+    out["at_plain64_relmse"] = None if best is None else {
+        "mode": best[0], "spp": best[1], "ms": best[2], "relmse": best[3],
+        "frame_time_ratio": round(p64["ms"] / best[2], 2)}
     return out
 
 
@@ -310,6 +423,8 @@ def run_ours(args):
     if not args.no_serving and world == 1:
         line["quality"] = quality_report(args)
         line["serving"] = serving_report(args)
+    if not args.no_cache and world == 1:
+        line["cache"] = cache_report(args, desc, scene, env, stream)
     peak, peak_kind = measured_peaks()
     sobol = nb.sobol_burley_table()
     if not args.no_cpu_baseline:

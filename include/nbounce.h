@@ -152,8 +152,11 @@ int nb_bvh_build(const float* positions, size_t n_vertices, const uint32_t* indi
  * ------------------------------------------------------------------------------------- */
 enum {
   /* Build one BLAS per distinct index range instead of one per primitive.  The reference
-   * builds one per glTF node-primitive (scene.rs:285-299); rebuilding an already built range
-   * reproduces the same tree, so traversal results are unchanged. */
+   * builds one per glTF node-primitive (scene.rs:285-299), rebuilding a shared range in place;
+   * those rebuilds are not idempotent (brute-force SAH ties resolve differently once the
+   * triangles are permuted), so the reference's first BLAS of a shared mesh can go stale
+   * against the final index buffer.  Without the flag the library reproduces that; with it
+   * every instance of a mesh uses one consistent tree. */
   NB_SCENE_DEDUP_MESHES = 1u << 0,
   /* Build and validate on the host only (no device needed, nothing uploaded): the scene can
    * be exported and inspected but not rendered or traced. */
@@ -233,6 +236,9 @@ int nb_pathtracer_last_stats(const nb_pathtracer* pt, uint64_t* rays, uint32_t* 
 typedef struct nb_kernel_times {
   double raygen_ms, trace_ms, shade_ms, accumulate_ms;
   uint64_t raygen_launches, trace_launches, shade_launches, accumulate_launches;
+  double cache_infer_ms;        /* radiance-cache lookups (cache mode only) */
+  double cache_train_ms;        /* training records + optimiser steps (cache mode only) */
+  uint64_t cache_infer_launches, cache_train_launches;
 } nb_kernel_times;
 int nb_pathtracer_enable_timing(nb_pathtracer* pt, int enable);
 /* Sums the recorded launch times (synchronises stream); reset != 0 clears the record. */
@@ -330,6 +336,84 @@ int nb_server_release(nb_server* server, uint64_t job_id);
 int nb_server_get_stats(nb_server* server, nb_server_stats* stats);
 /* Finishes the queued and active jobs, then stops the scheduler and frees its memory. */
 void nb_server_destroy(nb_server* server);
+
+/* ---------------------------------------------------------------------------------------
+ * Radiance cache.  No counterpart in the reference: its README lists neural radiance caching
+ * (Mueller et al. 2021) as planned work (README.md:12,23,50-53).  A 64 -> 5 x 64 (ReLU) -> 3
+ * MLP with BF16 weights/activations and FP32 accumulation, trained online on radiance from
+ * training paths the tracer extends, queried where the other paths end their prefix.
+ * Attach it to a path tracer with nb_pathtracer_set_cache; every render call is then one
+ * frame: its paths terminate into the cache and the call trains it.
+ * ------------------------------------------------------------------------------------- */
+#define NB_CACHE_PARAMS 21504   /* 5 x 64 x 64 + 16 x 64 weights, rows [out][in] per layer */
+#define NB_CACHE_INPUTS 64
+
+typedef struct nb_cache nb_cache;
+
+typedef struct nb_cache_config {
+  float learning_rate;          /* Adam step size (1e-2) */
+  float beta1, beta2, epsilon;  /* Adam (0.9, 0.99, 1e-8) */
+  float spread;                 /* end a path's prefix once its spread exceeds spread * a0
+                                   (0.01); < 0: at the primary hit; +inf: only at the last
+                                   bounce */
+  uint32_t train_records;       /* training records per frame (65,536); 0 with train_steps 0
+                                   freezes the cache */
+  uint32_t train_steps;         /* optimiser steps per frame over those records (4) */
+  uint32_t extra_vertices;      /* vertices a training path records past its query vertex (3) */
+  uint32_t seed;                /* weight initialisation */
+  float ema;                    /* renders query an exponential moving average of the weights
+                                   with this decay per step (0.99); 0: the weights themselves */
+  float grad_clip;              /* bound on |dloss/doutput| per record and channel (0: none);
+                                   limits the pull of rare very bright targets (sun hits) */
+} nb_cache_config;
+
+/* One cache input before encoding (64 bytes). */
+typedef struct nb_cache_vertex {
+  float pos[3];
+  float roughness;
+  float wo[3];                  /* unit direction towards the previous vertex */
+  float metallic;
+  float n[3];                   /* unit shading normal */
+  uint32_t tag;                 /* ignored */
+  float color[3];
+  float pad;
+} nb_cache_vertex;
+
+typedef struct nb_cache_stats {
+  uint64_t frames, adam_steps;
+  uint32_t queries;             /* cache lookups of the last frame (image + training tails) */
+  uint32_t records_found;       /* training records the last frame produced */
+  uint32_t records_used;        /* of which trained on (at most train_records) */
+  uint32_t training_groups;     /* groups of `stride` paths holding one training path each */
+  uint32_t stride;              /* group size for the next frame (adapted to the budget) */
+  float loss;                   /* mean relative L2 loss of the last frame's steps */
+} nb_cache_stats;
+
+void nb_cache_default_config(nb_cache_config* cfg);
+int nb_cache_create(const nb_cache_config* cfg /* NULL: defaults */, nb_cache** out);
+void nb_cache_destroy(nb_cache* cache);
+int nb_cache_get_config(const nb_cache* cache, nb_cache_config* out);
+/* Position normalisation box; defaults to the world bounds of the first scene rendered. */
+int nb_cache_set_bounds(nb_cache* cache, const float lo[3], const float hi[3]);
+/* FP32 master weights, NB_CACHE_PARAMS floats (host arrays).  Setting resets Adam. */
+int nb_cache_get_weights(const nb_cache* cache, float* weights, size_t n);
+int nb_cache_set_weights(nb_cache* cache, const float* weights, size_t n);
+/* The network's inputs of n vertices: device arrays, out is n x NB_CACHE_INPUTS floats. */
+int nb_cache_encode(nb_cache* cache, const nb_cache_vertex* vertices, size_t n, float* out, void* stream);
+/* Network outputs (n x 3) of encoded inputs (n x 64); device arrays, BF16 inside. */
+int nb_cache_infer(nb_cache* cache, const float* inputs, size_t n, float* out, void* stream);
+/* Mean gradient (NB_CACHE_PARAMS floats, device) and loss (host, may be NULL) of the relative
+ * L2 loss sum((p - y)^2 / (p^2 + 0.01)) / (3 n), the denominator held constant; targets n x 3.
+ * Synchronises stream. */
+int nb_cache_gradient(nb_cache* cache, const float* inputs, const float* targets, size_t n, float* grad,
+                      float* loss, void* stream);
+/* One Adam step on that loss over the batch.  Synchronises stream. */
+int nb_cache_train_step(nb_cache* cache, const float* inputs, const float* targets, size_t n, float* loss,
+                        void* stream);
+/* Counters of the last frame (synchronises stream). */
+int nb_cache_get_stats(nb_cache* cache, nb_cache_stats* out, void* stream);
+/* Renders with the cache (NULL: plain path tracing).  The cache must outlive the attachment. */
+int nb_pathtracer_set_cache(nb_pathtracer* pt, nb_cache* cache);
 
 #ifdef __cplusplus
 }

@@ -58,7 +58,27 @@ class NbSceneInfo(C.Structure):
 class NbKernelTimes(C.Structure):
     _fields_ = [("raygen_ms", C.c_double), ("trace_ms", C.c_double), ("shade_ms", C.c_double),
                 ("accumulate_ms", C.c_double), ("raygen_launches", C.c_uint64), ("trace_launches", C.c_uint64),
-                ("shade_launches", C.c_uint64), ("accumulate_launches", C.c_uint64)]
+                ("shade_launches", C.c_uint64), ("accumulate_launches", C.c_uint64), ("cache_infer_ms", C.c_double),
+                ("cache_train_ms", C.c_double), ("cache_infer_launches", C.c_uint64),
+                ("cache_train_launches", C.c_uint64)]
+
+
+NB_CACHE_PARAMS = 21504
+NB_CACHE_INPUTS = 64
+CACHE_VERTEX_DTYPE = np.dtype([("pos", "<f4", 3), ("roughness", "<f4"), ("wo", "<f4", 3), ("metallic", "<f4"),
+                               ("n", "<f4", 3), ("tag", "<u4"), ("color", "<f4", 3), ("pad", "<f4")])
+
+
+class NbCacheConfig(C.Structure):
+    _fields_ = [("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
+                ("spread", C.c_float), ("train_records", C.c_uint32), ("train_steps", C.c_uint32),
+                ("extra_vertices", C.c_uint32), ("seed", C.c_uint32), ("ema", C.c_float), ("grad_clip", C.c_float)]
+
+
+class NbCacheStats(C.Structure):
+    _fields_ = [("frames", C.c_uint64), ("adam_steps", C.c_uint64), ("queries", C.c_uint32),
+                ("records_found", C.c_uint32), ("records_used", C.c_uint32), ("training_groups", C.c_uint32),
+                ("stride", C.c_uint32), ("loss", C.c_float)]
 
 
 class NbJobDesc(C.Structure):
@@ -139,6 +159,19 @@ def lib():
         "nb_server_release": ([vp, u64], i32),
         "nb_server_get_stats": ([vp, vp], i32),
         "nb_server_destroy": ([vp], None),
+        "nb_cache_default_config": ([vp], None),
+        "nb_cache_create": ([vp, vp], i32),
+        "nb_cache_destroy": ([vp], None),
+        "nb_cache_get_config": ([vp, vp], i32),
+        "nb_cache_set_bounds": ([vp, vp, vp], i32),
+        "nb_cache_get_weights": ([vp, vp, sz], i32),
+        "nb_cache_set_weights": ([vp, vp, sz], i32),
+        "nb_cache_encode": ([vp, vp, sz, vp, vp], i32),
+        "nb_cache_infer": ([vp, vp, sz, vp, vp], i32),
+        "nb_cache_gradient": ([vp, vp, vp, sz, vp, vp, vp], i32),
+        "nb_cache_train_step": ([vp, vp, vp, sz, vp, vp], i32),
+        "nb_cache_get_stats": ([vp, vp, vp], i32),
+        "nb_pathtracer_set_cache": ([vp, vp], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

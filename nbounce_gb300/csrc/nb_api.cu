@@ -16,6 +16,7 @@
 #include <vector>
 
 #include "nb_internal.h"
+#include "nb_mlp.cuh"
 #include "nb_launch.h"
 #include "nb_runtime.h"
 
@@ -55,6 +56,7 @@ struct nb_pathtracer {
   std::unique_ptr<WaveTables> wt{new WaveTables()};  // kernel parameter tables (host copy)
   uint32_t capacity = 0;  // paths the work buffers hold
   uint32_t batch_paths = 1u << 27;
+  nb_cache* cache = nullptr;  // radiance-cache mode when set
   int sms = 1;
   // optional per-kernel event timing: (kind, start, stop) of every recorded launch
   bool timing = false;
@@ -62,7 +64,7 @@ struct nb_pathtracer {
   std::vector<std::tuple<int, cudaEvent_t, cudaEvent_t>> timed;
 };
 
-enum { kKindRaygen = 0, kKindTrace = 1, kKindShade = 2, kKindAccumulate = 3 };
+enum { kKindRaygen = 0, kKindTrace = 1, kKindShade = 2, kKindAccumulate = 3, kKindCacheInfer = 4, kKindCacheTrain = 5 };
 
 // Launches `launch` on st, bracketed by two events when timing is on.
 template <class F>
@@ -463,10 +465,32 @@ static int render_samples(nb_pathtracer* pt, const nb_scene* scene, const nb_cam
     wt.n_paths = npix * S;
     wt.n_pix = npix;
     const uint32_t B = pt->globals.bounces;
+    CacheWave cw{};
+    if (pt->cache) {
+      rc = cache_wave_begin(pt->cache, scene, wt.n_paths, &cw, st);
+      if (rc) return rc;
+    }
     cudaError_t e = timed_launch(pt, kKindRaygen, st, [&] { return launch_raygen(pb, wt, pt->sms, st); });
     for (uint32_t b = 0; b <= B && e == cudaSuccess; ++b) {
       e = timed_launch(pt, kKindTrace, st, [&] { return launch_trace_wave(pb, wt, true, b, pt->d_rays, pt->sms, st); });
-      if (e == cudaSuccess) e = timed_launch(pt, kKindShade, st, [&] { return launch_shade(pb, wt, b, pt->sms, st); });
+      if (e == cudaSuccess)
+        e = timed_launch(pt, kKindShade, st, [&] {
+          return pt->cache ? launch_shade_cache(pb, wt, cw, b, pt->sms, st) : launch_shade(pb, wt, b, pt->sms, st);
+        });
+    }
+    if (e == cudaSuccess && pt->cache) {
+      rc = NB_OK;
+      e = timed_launch(pt, kKindCacheInfer, st, [&] {
+        rc = cache_wave_infer(pt->cache, pb, pt->sms, st);
+        return cudaSuccess;
+      });
+      if (rc) return rc;
+      if (e == cudaSuccess)
+        e = timed_launch(pt, kKindCacheTrain, st, [&] {
+          rc = cache_wave_train(pt->cache, wt.n_paths, pt->sms, st);
+          return cudaSuccess;
+        });
+      if (rc) return rc;
     }
     if (e == cudaSuccess) e = timed_launch(pt, kKindAccumulate, st, [&] { return launch_accumulate(pb, wt, pt->sms, st); });
     if (e != cudaSuccess) return cuda_fail(e, "path batch launch");
@@ -503,8 +527,10 @@ int nb_pathtracer_kernel_times(nb_pathtracer* pt, nb_kernel_times* out, int rese
   if (!pt || !out) return fail(NB_ERR_INVALID_ARG, "NULL argument");
   NB_CUDA(cudaStreamSynchronize((cudaStream_t)stream), "cudaStreamSynchronize");
   std::memset(out, 0, sizeof(*out));
-  double* ms[4] = {&out->raygen_ms, &out->trace_ms, &out->shade_ms, &out->accumulate_ms};
-  uint64_t* cnt[4] = {&out->raygen_launches, &out->trace_launches, &out->shade_launches, &out->accumulate_launches};
+  double* ms[6] = {&out->raygen_ms, &out->trace_ms, &out->shade_ms, &out->accumulate_ms, &out->cache_infer_ms,
+                   &out->cache_train_ms};
+  uint64_t* cnt[6] = {&out->raygen_launches, &out->trace_launches, &out->shade_launches, &out->accumulate_launches,
+                      &out->cache_infer_launches, &out->cache_train_launches};
   for (auto& t : pt->timed) {
     float m = 0.0f;
     NB_CUDA(cudaEventSynchronize(std::get<2>(t)), "cudaEventSynchronize");
@@ -519,6 +545,12 @@ int nb_pathtracer_kernel_times(nb_pathtracer* pt, nb_kernel_times* out, int rese
     }
     pt->timed.clear();
   }
+  return NB_OK;
+}
+
+int nb_pathtracer_set_cache(nb_pathtracer* pt, nb_cache* cache) {
+  if (!pt) return fail(NB_ERR_INVALID_ARG, "NULL argument");
+  pt->cache = cache;
   return NB_OK;
 }
 

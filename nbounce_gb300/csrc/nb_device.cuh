@@ -95,6 +95,27 @@ __device__ __forceinline__ float4 hash4f(uint32_t x, uint32_t y) {
 
 __device__ __forceinline__ float fract(float x) { return x - floorf(x); }
 
+// atan2 / acos in binary32 by octant reduction and a degree-7 polynomial in x^2 for atan on
+// [0,1] (least-squares fit, max error 1.7e-7), Horner without fusion: the oracle
+// evaluates the identical sequence, so both sides agree bit for bit.
+__device__ __forceinline__ float nb_atan2(float y, float x) {
+  const float P[8] = {0x1.fffffcp-1f, -0x1.5551dp-2f, 0x1.98faep-3f, -0x1.1f1e82p-3f,
+                      0x1.96172p-4f,  -0x1.e75096p-5f, 0x1.8d5abp-6f, -0x1.3394dap-8f};
+  float ax = fabsf(x), ay = fabsf(y);
+  float mx = ax > ay ? ax : ay, mn = ax > ay ? ay : ax;
+  float a = mx > 0.0f ? mn / mx : 0.0f;
+  float a2 = a * a;
+  float p = P[7];
+#pragma unroll
+  for (int k = 6; k >= 0; --k) p = p * a2 + P[k];
+  float r = a * p;
+  if (ay > ax) r = 1.57079637f - r;
+  if (x < 0.0f) r = 3.14159274f - r;
+  if (y < 0.0f) r = -r;
+  return r;
+}
+__device__ __forceinline__ float nb_acos(float y) { return nb_atan2(sqrtf((1.0f - y) * (1.0f + y)), y); }
+
 // Device view of a scene (pointers into library-owned device memory).
 struct DevScene {
   const float4* tlas_wide;    // 5 float4 per 8-wide TLAS node; the root is node 0

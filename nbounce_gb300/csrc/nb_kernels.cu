@@ -29,6 +29,7 @@
 
 #include "nb_device.cuh"
 #include "nb_launch.h"
+#include "nb_mlp.cuh"
 
 namespace nbd {
 
@@ -368,27 +369,6 @@ __global__ void __launch_bounds__(128) k_trace_wave(PathBatch pb, const WaveTabl
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(ray_total, (unsigned long long)n);
 }
 
-// atan2 / acos in binary32 by octant reduction and a degree-7 polynomial in x^2 for atan on
-// [0,1] (fitted for this build, max error 1.7e-7), Horner without fusion: the oracle
-// evaluates the identical sequence, so both sides agree bit for bit.
-__device__ __forceinline__ float nb_atan2(float y, float x) {
-  const float P[8] = {0x1.fffffcp-1f, -0x1.5551dp-2f, 0x1.98faep-3f, -0x1.1f1e82p-3f,
-                      0x1.96172p-4f,  -0x1.e75096p-5f, 0x1.8d5abp-6f, -0x1.3394dap-8f};
-  float ax = fabsf(x), ay = fabsf(y);
-  float mx = ax > ay ? ax : ay, mn = ax > ay ? ay : ax;
-  float a = mx > 0.0f ? mn / mx : 0.0f;
-  float a2 = a * a;
-  float p = P[7];
-#pragma unroll
-  for (int k = 6; k >= 0; --k) p = p * a2 + P[k];
-  float r = a * p;
-  if (ay > ax) r = 1.57079637f - r;
-  if (x < 0.0f) r = 3.14159274f - r;
-  if (y < 0.0f) r = -r;
-  return r;
-}
-__device__ __forceinline__ float nb_acos(float y) { return nb_atan2(sqrtf((1.0f - y) * (1.0f + y)), y); }
-
 // equirect lookup (the oracle's definition): u = atan2(d.x, -d.z)/(2 pi) + 0.5, v = acos(d.y)/pi
 // of the normalised direction, bilinear with wrap in u and clamp in v; NaN directions see black
 __device__ V3 env_lookup(const DevEnv& env, V3 dir) {
@@ -455,6 +435,130 @@ __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool active) 
 }
 
 
+// Material and geometry of a hit (raytracing_sw.wgsl:138-173).  pos / nrm / tng are only
+// filled for non-emissive hits: an emissive hit ends the path (pathtracing.wgsl:172-174).
+struct HitSurface {
+  V3 color;
+  float roughness, metallic;
+  bool emissive;
+  V3 pos, nrm, tng;
+};
+
+__device__ __forceinline__ void load_hit_surface(const DevScene& s, uint32_t inst, float4 O, float4 H, V3 rdir,
+                                                 HitSurface& hs) {
+  const float4* sh = s.inst_shade + 6 * (size_t)inst;
+  const float4 c0 = ld4(sh), c1 = ld4(sh + 1), c2 = ld4(sh + 2);
+  const float4 l0 = ld4(sh + 3), l1 = ld4(sh + 4), l2 = ld4(sh + 5);
+  hs.color = V3{c0.w, c1.w, c2.w};
+  hs.roughness = l0.w;
+  hs.metallic = l1.w;
+  hs.emissive = l2.w > 0.0f;  // EMISSIVE (raytracing_sw.wgsl:168-170)
+  if (hs.emissive) return;
+  // hit attributes (raytracing_sw.wgsl:146-158)
+  const uint32_t tri = __float_as_uint(H.w);
+  const uint32_t i0 = __ldg(s.tri_idx + 3 * (size_t)tri), i1 = __ldg(s.tri_idx + 3 * (size_t)tri + 1),
+                 i2 = __ldg(s.tri_idx + 3 * (size_t)tri + 2);
+  const float4 a0 = ld4(s.vattr + 2 * (size_t)i0), a1 = ld4(s.vattr + 2 * (size_t)i1),
+               a2 = ld4(s.vattr + 2 * (size_t)i2);
+  const float4 b0 = ld4(s.vattr + 2 * (size_t)i0 + 1), b1 = ld4(s.vattr + 2 * (size_t)i1 + 1),
+               b2 = ld4(s.vattr + 2 * (size_t)i2 + 1);
+  const float u = H.y, v = H.z;
+  const float w0 = 1.0f - u - v;
+  const V3 ln = xyz(a0) * w0 + xyz(a1) * u + xyz(a2) * v;
+  const V3 lt = xyz(b0) * w0 + xyz(b1) * u + xyz(b2) * v;
+  hs.nrm = V3{dot(xyz(c0), ln), dot(xyz(c1), ln), dot(xyz(c2), ln)};
+  hs.tng = V3{dot(xyz(l0), lt), dot(xyz(l1), lt), dot(xyz(l2), lt)};
+  hs.pos = xyz(O) + H.x * rdir;
+}
+
+// Rotated Sobol samples of a bounce (pathtracing.wgsl:151-159, 176-178)
+__device__ __forceinline__ void bounce_samples(const PathBatch& pb, uint32_t sample, uint32_t bounce, float4 shift,
+                                               float4& s0, float4& s1) {
+  const uint32_t sb = sample * kLdsStride + 1u + bounce * kLdsPerBounce;
+  s0 = sobol_read(pb.sobol, pb.sobol_entries, sb);
+  s1 = sobol_read(pb.sobol, pb.sobol_entries, sb + 1u);
+  s0 = make_float4(fract(s0.x + shift.x), fract(s0.y + shift.y), fract(s0.z + shift.z), 0.0f);
+  s1 = make_float4(0.0f, fract(s1.y + shift.y), fract(s1.z + shift.z), 0.0f);
+}
+
+// Lobe choice and direction sampling at a non-emissive hit (pathtracing.wgsl:179-224).
+// weight is the factor the throughput is multiplied by.  With kPdf, pdf is the solid-angle
+// density of wi under the chosen lobe times its selection probability (used only by the
+// radiance cache's path-spread heuristic; +inf for a perfect mirror).
+struct BsdfSample {
+  V3 wi, weight, wo, n;
+  float cos_o, pdf;
+};
+
+template <bool kPdf>
+__device__ __forceinline__ BsdfSample sample_bsdf(const HitSurface& hs, V3 rdir, float4 s0, float4 s1) {
+  BsdfSample out;
+  const V3 color = hs.color;
+  const float roughness = hs.roughness, metallic = hs.metallic;
+  const float alpha = roughness * roughness;
+  const float alpha2 = alpha * alpha;
+  const V3 nn = normalize(hs.nrm);
+  const V3 wo = normalize(-rdir);
+  const float cosThetaO = dot(wo, nn);
+  V3 wi;
+  const V3 F0 = V3{0.04f, 0.04f, 0.04f} * (1.0f - metallic) + color * metallic;
+  const float specular_weight = luminance(F_schlick(dot(wo, nn), F0));
+  const float diffuse_weight = (1.0f - metallic) * luminance(color);
+  const float p_specular = specular_weight / (specular_weight + diffuse_weight);
+  const float p_diffuse = 1.0f - p_specular;
+  out.pdf = 0.0f;
+  if (s0.x < p_specular) {
+    const V3 wm = sample_vndf_iso(s0.y, s0.z, wo, alpha, nn);
+    const V3 ni = -wo;
+    wi = ni - (2.0f * dot(wm, ni)) * wm;  // reflect(-wo, wm)
+    const float cosThetaD = dot(wo, wm);
+    const float cosThetaI = dot(wi, nn);
+    const V3 F = F_schlick(cosThetaD, F0);
+    const float LambdaL = lambda_tr(cosThetaI, alpha2);
+    const float LambdaV = lambda_tr(cosThetaO, alpha2);
+    const V3 spec = F * (1.0f + LambdaV) / (1.0f + LambdaL + LambdaV);
+    out.weight = spec / p_specular;
+    if (kPdf) {
+      // VNDF reflection density: G1(wo) D(wm) / (4 cos_o), D the Trowbridge-Reitz NDF
+      const float nm = dot(nn, wm);
+      const float den = nm * nm * (alpha2 - 1.0f) + 1.0f;
+      const float D = alpha2 / (kPi * den * den);
+      out.pdf = alpha2 > 0.0f ? p_specular * D / (4.0f * (1.0f + LambdaV) * fabsf(cosThetaO))
+                              : __int_as_float(0x7f800000);
+    }
+  } else {
+    const V3 nt = normalize(hs.tng - dot(hs.tng, nn) * nn);  // build_tbn (common.wgsl:55-59)
+    const V3 bt = cross(nn, nt);
+    const float phi = kTwoPi * s1.y;
+    const float sinT = sqrtf(1.0f - s1.z);
+    const float cosT = sqrtf(s1.z);
+    float sp, cp;
+    nb_sincos(phi, &sp, &cp);
+    const V3 ls{cp * sinT, sp * sinT, cosT};
+    wi = nt * ls.x + bt * ls.y + nn * ls.z;
+    const V3 wm = normalize(wi + wo);
+    const float cosThetaD = dot(wi, wm);
+    const float cosThetaI = dot(wi, nn);
+    const float FD90 = 0.5f + 2.0f * alpha * pow2(cosThetaD);
+    const float response =
+        (1.0f + (FD90 - 1.0f) * pow5(1.0f - cosThetaI)) * (1.0f + (FD90 - 1.0f) * pow5(1.0f - cosThetaO));
+    const V3 diffuse = (1.0f - metallic) * color * response;
+    out.weight = diffuse / p_diffuse;
+    if (kPdf) out.pdf = p_diffuse * cosT * (1.0f / kPi);
+  }
+  out.wi = wi;
+  out.wo = wo;
+  out.n = nn;
+  out.cos_o = cosThetaO;
+  return out;
+}
+
+// Russian roulette probability (pathtracing.wgsl:225-236)
+__device__ __forceinline__ float rr_continue(uint32_t bounce, uint32_t bounces, V3 T, float cf) {
+  float p_continue = fminf(1.0f - pow8((float)bounce / (float)bounces), 1.0f);
+  return p_continue * fminf(luminance(T) * cf, 1.0f);
+}
+
 __global__ void __launch_bounds__(256) k_shade(PathBatch pb, const WaveTables wt, uint32_t bounce) {
   __shared__ Segment segs[nb::kMaxWaveSegments];
   stage_segments(segs, wt);
@@ -484,90 +588,25 @@ __global__ void __launch_bounds__(256) k_shade(PathBatch pb, const WaveTables wt
         const V3 L = T * env_lookup(jp.env, rdir);
         pb.radiance[id] = make_float4(L.x, L.y, L.z, 0.0f);
       } else {
-        const uint32_t inst = pb.hit_inst[i];
-        const float4* sh = s.inst_shade + 6 * (size_t)inst;
-        const float4 c0 = ld4(sh), c1 = ld4(sh + 1), c2 = ld4(sh + 2);
-        const float4 l0 = ld4(sh + 3), l1 = ld4(sh + 4), l2 = ld4(sh + 5);
-        const V3 color{c0.w, c1.w, c2.w};
-        if (l2.w > 0.0f) {  // EMISSIVE (raytracing_sw.wgsl:168-170, pathtracing.wgsl:172-174)
-          const V3 L = T * color;
+        HitSurface hs;
+        load_hit_surface(s, pb.hit_inst[i], O, H, rdir, hs);
+        if (hs.emissive) {  // pathtracing.wgsl:172-174
+          const V3 L = T * hs.color;
           pb.radiance[id] = make_float4(L.x, L.y, L.z, 0.0f);
         } else {
-          // hit attributes (raytracing_sw.wgsl:146-158)
-          const uint32_t tri = __float_as_uint(H.w);
-          const uint32_t i0 = __ldg(s.tri_idx + 3 * (size_t)tri), i1 = __ldg(s.tri_idx + 3 * (size_t)tri + 1),
-                         i2 = __ldg(s.tri_idx + 3 * (size_t)tri + 2);
-          const float4 a0 = ld4(s.vattr + 2 * (size_t)i0), a1 = ld4(s.vattr + 2 * (size_t)i1),
-                       a2 = ld4(s.vattr + 2 * (size_t)i2);
-          const float4 b0 = ld4(s.vattr + 2 * (size_t)i0 + 1), b1 = ld4(s.vattr + 2 * (size_t)i1 + 1),
-                       b2 = ld4(s.vattr + 2 * (size_t)i2 + 1);
-          const float u = H.y, v = H.z;
-          const float w0 = 1.0f - u - v;
-          const V3 ln = xyz(a0) * w0 + xyz(a1) * u + xyz(a2) * v;
-          const V3 lt = xyz(b0) * w0 + xyz(b1) * u + xyz(b2) * v;
-          const V3 nrm{dot(xyz(c0), ln), dot(xyz(c1), ln), dot(xyz(c2), ln)};
-          const V3 tng{dot(xyz(l0), lt), dot(xyz(l1), lt), dot(xyz(l2), lt)};
-          const V3 pos = xyz(O) + H.x * rdir;
-
           const uint32_t local = id - sg.path_begin;
           const uint32_t pix = local % jp.npix;
           const uint32_t sample = sg.first_sample + local / jp.npix;
-          const float4 shift = hash4f(pix % jp.width, pix / jp.width);
-          const float roughness = l0.w, metallic = l1.w;
-          const float alpha = roughness * roughness;
-          const float alpha2 = alpha * alpha;
-          const V3 nn = normalize(nrm);
-          const uint32_t sb = sample * kLdsStride + 1u + bounce * kLdsPerBounce;
-          float4 s0 = sobol_read(pb.sobol, pb.sobol_entries, sb);
-          float4 s1 = sobol_read(pb.sobol, pb.sobol_entries, sb + 1u);
-          s0 = make_float4(fract(s0.x + shift.x), fract(s0.y + shift.y), fract(s0.z + shift.z), 0.0f);
-          s1 = make_float4(0.0f, fract(s1.y + shift.y), fract(s1.z + shift.z), 0.0f);
-          const V3 wo = normalize(-rdir);
-          const float cosThetaO = dot(wo, nn);
-          V3 wi;
-          const V3 F0 = V3{0.04f, 0.04f, 0.04f} * (1.0f - metallic) + color * metallic;
-          const float specular_weight = luminance(F_schlick(dot(wo, nn), F0));
-          const float diffuse_weight = (1.0f - metallic) * luminance(color);
-          const float p_specular = specular_weight / (specular_weight + diffuse_weight);
-          const float p_diffuse = 1.0f - p_specular;
-          if (s0.x < p_specular) {
-            const V3 wm = sample_vndf_iso(s0.y, s0.z, wo, alpha, nn);
-            const V3 ni = -wo;
-            wi = ni - (2.0f * dot(wm, ni)) * wm;  // reflect(-wo, wm)
-            const float cosThetaD = dot(wo, wm);
-            const float cosThetaI = dot(wi, nn);
-            const V3 F = F_schlick(cosThetaD, F0);
-            const float LambdaL = lambda_tr(cosThetaI, alpha2);
-            const float LambdaV = lambda_tr(cosThetaO, alpha2);
-            const V3 spec = F * (1.0f + LambdaV) / (1.0f + LambdaL + LambdaV);
-            T = T * (spec / p_specular);
-          } else {
-            const V3 nt = normalize(tng - dot(tng, nn) * nn);  // build_tbn (common.wgsl:55-59)
-            const V3 bt = cross(nn, nt);
-            const float phi = kTwoPi * s1.y;
-            const float sinT = sqrtf(1.0f - s1.z);
-            const float cosT = sqrtf(s1.z);
-            float sp, cp;
-            nb_sincos(phi, &sp, &cp);
-            const V3 ls{cp * sinT, sp * sinT, cosT};
-            wi = nt * ls.x + bt * ls.y + nn * ls.z;
-            const V3 wm = normalize(wi + wo);
-            const float cosThetaD = dot(wi, wm);
-            const float cosThetaI = dot(wi, nn);
-            const float FD90 = 0.5f + 2.0f * alpha * pow2(cosThetaD);
-            const float response =
-                (1.0f + (FD90 - 1.0f) * pow5(1.0f - cosThetaI)) * (1.0f + (FD90 - 1.0f) * pow5(1.0f - cosThetaO));
-            const V3 diffuse = (1.0f - metallic) * color * response;
-            T = T * (diffuse / p_diffuse);
-          }
-          // Russian roulette (pathtracing.wgsl:225-236)
-          float p_continue = fminf(1.0f - pow8((float)bounce / (float)jp.bounces), 1.0f);
-          p_continue = p_continue * fminf(luminance(T) * jp.cf, 1.0f);
+          float4 s0, s1;
+          bounce_samples(pb, sample, bounce, hash4f(pix % jp.width, pix / jp.width), s0, s1);
+          const BsdfSample bs = sample_bsdf<false>(hs, rdir, s0, s1);
+          T = T * bs.weight;
+          const float p_continue = rr_continue(bounce, jp.bounces, T, jp.cf);
           if (s0.z < p_continue && bounce < jp.bounces) {
             T = T / p_continue;
             cont = true;
-            next_o = make_float4(pos.x, pos.y, pos.z, O.w);
-            next_d = make_float4(wi.x, wi.y, wi.z, D.w);
+            next_o = make_float4(hs.pos.x, hs.pos.y, hs.pos.z, O.w);
+            next_d = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, D.w);
             next_t = make_float4(T.x, T.y, T.z, 0.0f);
           }
         }
@@ -578,6 +617,189 @@ __global__ void __launch_bounds__(256) k_shade(PathBatch pb, const WaveTables wt
       out_o[slot] = next_o;
       out_d[slot] = next_d;
       out_t[slot] = next_t;
+    }
+  }
+}
+
+// 32-bit integer finaliser (Wellons' lowbias32)
+__device__ __forceinline__ uint32_t mix32(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+__device__ __forceinline__ nb::CacheFeatures cache_features(const HitSurface& hs, const BsdfSample& bs, uint32_t tag) {
+  nb::CacheFeatures f;
+  f.pos[0] = hs.pos.x; f.pos[1] = hs.pos.y; f.pos[2] = hs.pos.z;
+  f.roughness = hs.roughness;
+  f.wo[0] = bs.wo.x; f.wo[1] = bs.wo.y; f.wo[2] = bs.wo.z;
+  f.metallic = hs.metallic;
+  f.n[0] = bs.n.x; f.n[1] = bs.n.y; f.n[2] = bs.n.z;
+  f.tag = tag;
+  f.color[0] = hs.color.x; f.color[1] = hs.color.y; f.color[2] = hs.color.z;
+  f.pad = 0.0f;
+  return f;
+}
+
+// Shade for the radiance-cache mode.  The prefix of every path is the plain tracer's (same
+// samples, lobes and Russian roulette); what changes is where it ends:
+//  - path spread (Mueller et al. 2021, sec. 3.3): a0 = |x0 - x1|^2 / (4 pi cos1) at the
+//    primary hit, and sqrt a(x1..xn) = sum_{i>=2} |x_{i-1} - x_i| / sqrt(p_{i-1} cos_i), with
+//    p the density of the sampled direction.  At the first vertex where sqrt a > sqrt(c a0)
+//    (or at the last bounce) the path becomes an image query: its sample is T * cache(x).
+//  - one path per group of `stride` path ids (position in the group hashed from the group
+//    and the frame) is a training path: it records each vertex (features and the factor its
+//    throughput is multiplied by), continues past its query vertex for `extra` vertices and
+//    ends in a tail query that closes its radiance chain with the cache (self-training),
+//    unless a miss, an emitter or Russian roulette ends it first.
+__global__ void __launch_bounds__(256) k_shade_cache(PathBatch pb, const WaveTables wt, const nb::CacheWave cw,
+                                                     uint32_t bounce) {
+  using nb::CacheQuery;
+  __shared__ Segment segs[nb::kMaxWaveSegments];
+  stage_segments(segs, wt);
+  const uint32_t n = pb.counts[bounce];
+  const bool odd = (bounce & 1) != 0;
+  const float4* __restrict__ in_o = odd ? pb.q_o[1] : pb.q_o[0];
+  const float4* __restrict__ in_d = odd ? pb.q_d[1] : pb.q_d[0];
+  const float4* __restrict__ in_t = odd ? pb.q_t[1] : pb.q_t[0];
+  const float4* __restrict__ in_x = odd ? cw.q_x[1] : cw.q_x[0];
+  float4* __restrict__ out_o = odd ? pb.q_o[0] : pb.q_o[1];
+  float4* __restrict__ out_d = odd ? pb.q_d[0] : pb.q_d[1];
+  float4* __restrict__ out_t = odd ? pb.q_t[0] : pb.q_t[1];
+  float4* __restrict__ out_x = odd ? cw.q_x[0] : cw.q_x[1];
+  const uint32_t G = *cw.stride;
+  const uint32_t frame_key = mix32(cw.frame ^ 0x5bd1e995u);
+  const uint32_t stride = gridDim.x * blockDim.x;
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    bool cont = false, image_q = false, tail_q = false;
+    float4 next_o = make_float4(0.f, 0.f, 0.f, 0.f), next_d = next_o, next_t = next_o, next_x = next_o;
+    nb::CacheFeatures f{};
+    V3 Tq3{0.0f, 0.0f, 0.0f};
+    uint32_t slot = ~0u;
+    if (i < n) {
+      const float4 O = in_o[i], D = in_d[i], Tq = in_t[i], H = pb.hits[i];
+      const uint32_t id = __float_as_uint(O.w);
+      const Segment sg = segs[find_segment<false>(segs, wt.n_segs, id)];
+      const JobParams& jp = wt.jobs[sg.job];
+      const DevScene& s = wt.scenes[jp.scene];
+      V3 T = xyz(Tq);
+      const V3 rdir = xyz(D);
+      float budget = 0.0f, pdf_prev = 0.0f;
+      uint32_t flags = 0;
+      if (bounce == 0) {
+        const uint32_t group = id / G;
+        const bool train = group < cw.max_slots && id % G == mix32(group ^ frame_key) % G;
+        slot = train ? group : ~0u;
+        flags = train ? nb::kPathTraining : 0u;
+      } else {
+        const float4 X = in_x[i];
+        budget = X.x;
+        pdf_prev = X.y;
+        slot = __float_as_uint(X.z);
+        flags = __float_as_uint(X.w);
+      }
+      const bool training = (flags & nb::kPathTraining) != 0;
+      const bool image_done = (flags & nb::kPathImageDone) != 0;
+      if (H.x == kNoHit) {
+        const V3 E = env_lookup(jp.env, rdir);
+        if (!image_done) {
+          const V3 L = T * E;
+          pb.radiance[id] = make_float4(L.x, L.y, L.z, 0.0f);
+        }
+        if (training) cw.tail[slot] = make_float4(E.x, E.y, E.z, 0.0f);
+      } else {
+        HitSurface hs;
+        load_hit_surface(s, pb.hit_inst[i], O, H, rdir, hs);
+        if (hs.emissive) {
+          if (!image_done) {
+            const V3 L = T * hs.color;
+            pb.radiance[id] = make_float4(L.x, L.y, L.z, 0.0f);
+          }
+          if (training) cw.tail[slot] = make_float4(hs.color.x, hs.color.y, hs.color.z, 0.0f);
+        } else {
+          const uint32_t local = id - sg.path_begin;
+          const uint32_t pix = local % jp.npix;
+          const uint32_t sample = sg.first_sample + local / jp.npix;
+          float4 s0, s1;
+          bounce_samples(pb, sample, bounce, hash4f(pix % jp.width, pix / jp.width), s0, s1);
+          const BsdfSample bs = sample_bsdf<true>(hs, rdir, s0, s1);
+          const float dist2 = H.x * H.x * dot(rdir, rdir);
+          const float cos_v = fabsf(bs.cos_o);
+          if (bounce == 0)
+            budget = cw.spread_c < 0.0f ? -1.0f : sqrtf(cw.spread_c * dist2 / (4.0f * kPi * cos_v));
+          else
+            budget = budget - sqrtf(dist2 / (pdf_prev * cos_v));
+          f = cache_features(hs, bs, id);
+          Tq3 = T;
+          const V3 Tn = T * bs.weight;
+          const float p_continue = rr_continue(bounce, jp.bounces, Tn, jp.cf);
+          const bool rr_ok = s0.z < p_continue && bounce < jp.bounces;
+          // an infinite c turns the spread rule off; otherwise NaN budgets (degenerate
+          // geometry) end the prefix as well
+          const bool spread_end = !isinf(cw.spread_c) && !(budget >= 0.0f);
+          image_q = !image_done && (spread_end || bounce >= jp.bounces);
+          bool go = false;
+          if (!training) {
+            go = !image_q && rr_ok;
+          } else {
+            uint32_t since = (flags >> nb::kPathSinceShift) & 0xFFu;
+            // a training path that reaches the vertex cap ends here, its pixel sample included
+            if (bounce >= nb::kCacheMaxVertices) image_q = !image_done;
+            if (image_q) {
+              flags |= nb::kPathImageDone;
+              since = 0;
+            }
+            if (((flags & nb::kPathImageDone) && since >= cw.extra) || bounce >= nb::kCacheMaxVertices) {
+              tail_q = true;
+            } else {
+              const V3 w = rr_ok ? bs.weight / p_continue : V3{0.0f, 0.0f, 0.0f};
+              nb::TrainVertex tv;
+              tv.f = f;
+              tv.w = make_float4(w.x, w.y, w.z, 0.0f);
+              cw.verts[(size_t)slot * nb::kCacheMaxVertices + bounce] = tv;
+              cw.vert_count[slot] = bounce + 1;
+              go = rr_ok;
+              if (!go) cw.tail[slot] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+              if (go && (flags & nb::kPathImageDone)) since += 1;
+            }
+            flags = (flags & 0xFFu) | (since << nb::kPathSinceShift);
+          }
+          if (go) {
+            const V3 Tc = Tn / p_continue;
+            cont = true;
+            next_o = make_float4(hs.pos.x, hs.pos.y, hs.pos.z, O.w);
+            next_d = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, D.w);
+            next_t = make_float4(Tc.x, Tc.y, Tc.z, 0.0f);
+            next_x = make_float4(budget, bs.pdf, __uint_as_float(slot), __uint_as_float(flags));
+          }
+        }
+      }
+    }
+    const uint32_t at = warp_append(pb.counts + bounce + 1, cont);
+    if (cont) {
+      out_o[at] = next_o;
+      out_d[at] = next_d;
+      out_t[at] = next_t;
+      out_x[at] = next_x;
+    }
+    const uint32_t qi = warp_append(cw.n_queries, image_q);
+    if (image_q && qi < cw.max_queries) {
+      CacheQuery q;
+      q.f = f;
+      q.T = make_float4(Tq3.x, Tq3.y, Tq3.z, 0.0f);
+      cw.queries[qi] = q;
+    }
+    const uint32_t ti = warp_append(cw.n_queries, tail_q);
+    if (tail_q && ti < cw.max_queries) {
+      CacheQuery q;
+      q.f = f;
+      q.f.tag = nb::kCacheTailBit | slot;
+      q.T = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
+      cw.queries[ti] = q;
     }
   }
 }
@@ -653,6 +875,13 @@ cudaError_t launch_trace_wave(const PathBatch& pb, const WaveTables& wt, bool si
 cudaError_t launch_shade(const PathBatch& pb, const WaveTables& wt, uint32_t bounce, int sms, cudaStream_t st) {
   static const int g = blocks_for((const void*)nbd::k_shade, 256, sms);
   nbd::k_shade<<<g, 256, 0, st>>>(pb, wt, bounce);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shade_cache(const PathBatch& pb, const WaveTables& wt, const CacheWave& cw, uint32_t bounce,
+                               int sms, cudaStream_t st) {
+  static const int g = blocks_for((const void*)nbd::k_shade_cache, 256, sms);
+  nbd::k_shade_cache<<<g, 256, 0, st>>>(pb, wt, cw, bounce);
   return cudaGetLastError();
 }
 

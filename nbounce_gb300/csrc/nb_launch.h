@@ -69,6 +69,10 @@ cudaError_t launch_raygen(const PathBatch& pb, const WaveTables& wt, int sms, cu
 cudaError_t launch_trace_wave(const PathBatch& pb, const WaveTables& wt, bool single_scene, uint32_t bounce,
                               unsigned long long* ray_total, int sms, cudaStream_t st);
 cudaError_t launch_shade(const PathBatch& pb, const WaveTables& wt, uint32_t bounce, int sms, cudaStream_t st);
+struct CacheWave;
+// radiance-cache mode shade (nb_mlp.cuh describes the wave state)
+cudaError_t launch_shade_cache(const PathBatch& pb, const WaveTables& wt, const CacheWave& cw, uint32_t bounce,
+                               int sms, cudaStream_t st);
 cudaError_t launch_accumulate(const PathBatch& pb, const WaveTables& wt, int sms, cudaStream_t st);
 
 }  // namespace nb

@@ -78,3 +78,14 @@ struct nb_env {
   nbd::DevEnv dev{};
   nb::DeviceArena arena;
 };
+
+// radiance-cache mode of a wave (nb_cache.cu)
+namespace nb {
+struct CacheWave;
+// before raygen: buffers, counters and the wave state read by launch_shade_cache
+int cache_wave_begin(nb_cache* c, const nb_scene* scene, uint32_t n_paths, CacheWave* cw, cudaStream_t st);
+// after the last bounce: cache lookups (image queries and training-path tails)
+int cache_wave_infer(nb_cache* c, const PathBatch& pb, int sms, cudaStream_t st);
+// then: training records and optimiser steps
+int cache_wave_train(nb_cache* c, uint32_t n_paths, int sms, cudaStream_t st);
+}  // namespace nb

@@ -259,6 +259,11 @@ class Pathtracer:
     def set_batch_paths(self, paths):
         check(lib().nb_pathtracer_set_batch_paths(self._h, int(paths)))
 
+    def set_cache(self, cache):
+        """Attach a RadianceCache (None: plain path tracing).  Keep the cache alive meanwhile."""
+        self._cache = cache
+        check(lib().nb_pathtracer_set_cache(self._h, None if cache is None else cache.handle))
+
     def enable_timing(self, enable=True):
         check(lib().nb_pathtracer_enable_timing(self._h, int(enable)))
 

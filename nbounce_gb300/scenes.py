@@ -280,6 +280,70 @@ def spheres_scene(seed=0x5EED0, n_spheres=64, subdiv=3, width=256, height=256, s
     return SceneDesc(v, i, meshes, insts, width, height, c2w, w2c, (0.5, 0.6, 0.8), None, bounces, spp)
 
 
+def quad_mesh(center, eu, ev):
+    """Two triangles spanning center +- eu +- ev; front face (the side the backface-culled
+    intersection test accepts) towards eu x ev."""
+    c, eu, ev = (np.asarray(a, np.float64) for a in (center, eu, ev))
+    pos = np.array([c - eu - ev, c + eu - ev, c - eu + ev, c + eu + ev])
+    n = np.cross(eu, ev)
+    n /= np.linalg.norm(n)
+    t = eu / np.linalg.norm(eu)
+    faces = np.array([[0, 1, 2], [1, 3, 2]], np.uint32)
+    return pack_vertices(pos, np.tile(n, (4, 1)), np.tile([*t, 1.0], (4, 1))), faces
+
+
+def room_scene(width=128, height=128, spp=16, bounces=8, light=(15.0, 15.0, 13.0)):
+    """A closed 10 x 10 x 10 room lit only by an emissive ceiling panel: red and green side
+    walls, white floor, ceiling and end walls, a diffuse and a rough gold sphere.  Radiance
+    reaches most pixels after several diffuse bounces (interreflection-dominated)."""
+    b = _Builder()
+    walls = [  # (center, eu, ev, colour): front faces point into the room
+        ((0, 0, 0), (5, 0, 0), (0, 0, -5), (0.75, 0.75, 0.75)),    # floor
+        ((0, 10, 0), (5, 0, 0), (0, 0, 5), (0.75, 0.75, 0.75)),    # ceiling
+        ((0, 5, -5), (5, 0, 0), (0, 5, 0), (0.75, 0.75, 0.75)),    # back
+        ((0, 5, 5), (0, 5, 0), (5, 0, 0), (0.75, 0.75, 0.75)),     # front
+        ((-5, 5, 0), (0, 5, 0), (0, 0, 5), (0.75, 0.12, 0.10)),    # left
+        ((5, 5, 0), (0, 0, 5), (0, 5, 0), (0.12, 0.70, 0.12)),     # right
+    ]
+    insts = []
+    for c, eu, ev, col in walls:
+        m = b.add_mesh(*quad_mesh(c, eu, ev))
+        insts.append(_instance(m, np.eye(4), dict(color=np.array([*col, 1.0], np.float32), roughness=np.float32(0.9),
+                                                  metallic=np.float32(0.0), emissive=np.float32(0.0))))
+    lm = b.add_mesh(*quad_mesh((0, 9.95, 0), (1.5, 0, 0), (0, 0, 1.5)))
+    insts.append(_instance(lm, np.eye(4), dict(color=np.array([*light, 1.0], np.float32), roughness=np.float32(1.0),
+                                               metallic=np.float32(0.0), emissive=np.float32(1.0))))
+    pos, faces = icosphere(4)
+    sph = b.add_mesh(pack_vertices(pos, pos, sphere_tangents(pos)), faces)
+    insts.append(_instance(sph, trs((-2.0, 1.8, -1.5), None, 1.8),
+                           dict(color=np.array([0.8, 0.8, 0.8, 1.0], np.float32), roughness=np.float32(0.8),
+                                metallic=np.float32(0.0), emissive=np.float32(0.0))))
+    insts.append(_instance(sph, trs((2.2, 1.5, 1.0), None, 1.5),
+                           dict(color=np.array([1.0, 0.78, 0.34, 1.0], np.float32), roughness=np.float32(0.25),
+                                metallic=np.float32(1.0), emissive=np.float32(0.0))))
+    v, i, meshes = b.finish()
+    w2c, c2w = camera_matrices((0.0, 5.0, 4.6), (0.0, 4.0, -5.0), width, height)
+    return SceneDesc(v, i, meshes, insts, width, height, c2w, w2c, (0.0, 0.0, 0.0), None, bounces, spp)
+
+
+def camera_path(n_frames, seed=0x5EEDC, eye=(0.0, 14.0, 62.0), target=(0.0, -2.0, 0.0), eye_spread=(16.0, 5.0, 10.0),
+                target_spread=(4.0, 1.5, 4.0), n_keys=6):
+    """Seeded camera spline: n_frames (eye, target) pairs on Catmull-Rom curves through n_keys
+    random keys around eye / target (clamped end tangents; the last frame sits on the last key)."""
+    rng = np.random.default_rng(seed)
+    ke = np.asarray(eye, np.float64) + rng.uniform(-1.0, 1.0, (n_keys, 3)) * np.asarray(eye_spread)
+    kt = np.asarray(target, np.float64) + rng.uniform(-1.0, 1.0, (n_keys, 3)) * np.asarray(target_spread)
+
+    def catmull_rom(P, u):
+        i = min(int(u), n_keys - 2)
+        t = u - i
+        p0, p1, p2, p3 = P[max(i - 1, 0)], P[i], P[i + 1], P[min(i + 2, n_keys - 1)]
+        return 0.5 * (2.0 * p1 + (p2 - p0) * t + (2.0 * p0 - 5.0 * p1 + 4.0 * p2 - p3) * t * t
+                      + (3.0 * p1 - p0 - 3.0 * p2 + p3) * t * t * t)
+
+    return [(catmull_rom(ke, u), catmull_rom(kt, u)) for u in np.linspace(0.0, n_keys - 1.0, n_frames)]
+
+
 def sky_envmap(seed, width=2048, height=1024, sun_dir=(0.3, 0.8, -0.52), sun_radiance=1.0e4,
                sun_diameter_deg=0.5):
     """Equirect RGBA32F sky: lognormal(0, 1.5) radiance field (smooth) + one sun disc."""

@@ -1,7 +1,7 @@
 // CPU oracle for the nBounce path-tracing pass.
 //
 // TEST INFRASTRUCTURE ONLY: tests/, __graft_entry__.smoke() and bench.py's CPU
-// baseline leg load this library as the checker.  The product (nbounce_gb300)
+// baseline leg load this library as the reference for parity checks.  The product (nbounce_gb300)
 // never links, loads or calls it.
 //
 // This file restates, operation for operation, the reference algorithm of julcst/nbounce:
@@ -868,7 +868,7 @@ static V3<R> sample_rendering_eq(const RenderArgs& a, uint32_t sample, const flo
 // Equirect lookup (the build's definition; the reference samples a cube map): on the
 // normalised direction d, u = atan2(d.x, -d.z) / (2 pi) + 0.5 and v = acos(d.y) / pi; bilinear
 // filtering with wrap in u and clamp in v, texel centres at (i + 0.5) / size; a NaN direction
-// sees black.  binary32: atan on [0,1] is x * P(x^2) with a degree-7 P fitted for this build
+// sees black.  binary32: atan on [0,1] is x * P(x^2) with a least-squares fitted degree-7 P
 // (max error 1.7e-7), atan2/acos by octant reduction, Horner without fusion.  binary64 (truth
 // mode): libm atan2/acos.
 constexpr float kAtanP[8] = {0x1.fffffcp-1f, -0x1.5551dp-2f, 0x1.98faep-3f, -0x1.1f1e82p-3f,
