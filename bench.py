@@ -62,6 +62,9 @@ def parse():
     p.add_argument("--serving-loads", type=str, default="10:60,30:90,60:120",
                    help="rate:jobs pairs of Poisson loads for the serving report")
     p.add_argument("--no-cache", action="store_true", help="skip the radiance-cache report")
+    p.add_argument("--all-configs", action="store_true",
+                   help="instead of the benchmark line, measure the other workloads (spheres 256x256 16 spp, "
+                        "1M-triangle soup traversal) on GPU and CPU and print them as one JSON line")
     p.add_argument("--cache-frames", type=int, default=300, help="1-spp frames of online training on the camera path")
     p.add_argument("--cache-ref-spp", type=int, default=16384, help="samples of the cache report's reference image")
     return p.parse_args()
@@ -166,10 +169,18 @@ def cpu_baseline(desc, sobol, seconds, threads):
 
 
 def rel_mse(img, ref):
-    """mean over pixels and channels of (x - ref)^2 / (ref^2 + 1e-2)"""
+    """mean over pixels and channels of (x - ref)^2 / (ref^2 + 1e-2), over the pixels where both
+    images are finite: the reference shading divides 0 by 0 at exactly grazing angles
+    (pathtracing.wgsl:119-125 with cos = 0), and a NaN sample stays in a pixel's running mean,
+    so a long reference render can hold a few NaN pixels (counted by nonfinite_pixels)."""
     x = img[..., :3].astype(np.float64)
     r = ref[..., :3].astype(np.float64)
-    return float(np.mean((x - r) ** 2 / (r * r + 1e-2)))
+    ok = np.all(np.isfinite(x), axis=-1) & np.all(np.isfinite(r), axis=-1)
+    return float(np.mean(((x - r) ** 2 / (r * r + 1e-2))[ok]))
+
+
+def nonfinite_pixels(img):
+    return int(np.sum(~np.all(np.isfinite(img[..., :3]), axis=-1)))
 
 
 def quality_report(args, ref_spp=16384, width=480, height=270):
@@ -323,6 +334,85 @@ def cache_report(args, desc, scene, env, stream):
     out["at_plain64_relmse"] = None if best is None else {
         "mode": best[0], "spp": best[1], "ms": best[2], "relmse": best[3],
         "frame_time_ratio": round(p64["ms"] / best[2], 2)}
+    return out
+
+
+def configs_report(args):
+    """GPU and CPU (oracle, all host threads) numbers of the two other workloads:
+    spheres: 64 icospheres + ground, 256x256, 16 spp, 6 bounces, constant sky; Mrays/s, frame
+             ms and relMSE against a 16,384-spp render of the same frame
+    soup:    1M-triangle soup (edges ~0.02 in [-1,1]^3), 16,777,216 rays, coherent (1024 x 16384
+             pinhole grid) and incoherent (uniform origins and directions), closest and any hit;
+             GPU on device-resident rays, CPU on a 262,144-ray prefix of the same rays."""
+    import torch
+    import nbounce_gb300 as nb
+    from nbounce_gb300 import scenes
+    from oracle import oracle as O
+    threads = os.cpu_count() or 1
+    out = {"cpu_threads": threads}
+    # spheres
+    desc = scenes.spheres_scene(width=256, height=256, spp=16, bounces=6)
+    scene = nb.SceneBuffers.from_desc(desc)
+    env = nb.EnvMap(desc.env_color)
+    cam = nb.camera_struct(desc.world_to_clip, desc.clip_to_world)
+    ref_pt = nb.Pathtracer(256, 256, nb.Globals(bounces=6), sobol_table=nb.sobol_burley_table(16384, 17))
+    ref_pt.render(scene, cam, env, 16384)
+    ref = ref_pt.download()
+    pt = nb.Pathtracer(256, 256, nb.Globals(bounces=6))
+    for _ in range(3):
+        pt.invalidate()
+        pt.render(scene, cam, env, 16)
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    a.record()
+    for _ in range(10):
+        pt.invalidate()
+        pt.render(scene, cam, env, 16)
+    b.record()
+    b.synchronize()
+    ms = a.elapsed_time(b) / 10
+    rays, _ = pt.last_stats()
+    img = pt.download()
+    osc = O.OracleScene(desc.vertices, desc.indices, desc.primitives(), dedup=True)
+    t = time.perf_counter()
+    cimg, crays, _, _ = osc.render(desc.clip_to_world, 256, 256, nb.sobol_burley_table(), 1, 16, bounces=6,
+                                   env=desc.env_color, threads=threads)
+    cs = time.perf_counter() - t
+    out["spheres_256_16spp"] = {
+        "gpu": {"mrays_s": round(rays / ms / 1e3, 1), "frame_ms": round(ms, 3), "rays": int(rays),
+                "relmse": round(rel_mse(img, ref), 5), "nonfinite_pixels": nonfinite_pixels(img)},
+        "cpu": {"mrays_s": round(crays / cs / 1e6, 2), "frame_ms": round(cs * 1e3, 1), "rays": int(crays),
+                "relmse": round(rel_mse(cimg, ref), 5), "nonfinite_pixels": nonfinite_pixels(cimg)},
+        "reference": "16,384-spp plain GPU render", "reference_nonfinite_pixels": nonfinite_pixels(ref)}
+    # soup traversal
+    desc = scenes.soup_scene(1 << 20)
+    soup = nb.SceneBuffers.from_desc(desc)
+    osc = O.OracleScene(desc.vertices, desc.indices, desc.primitives(), dedup=True)
+    n = 1 << 24
+    res = {}
+    for kind in ("coherent", "incoherent"):
+        rays = scenes.coherent_rays(1024, 16384) if kind == "coherent" else scenes.incoherent_rays(n, seed=0x5EED3)
+        d_rays = torch.from_numpy(rays).cuda()
+        hits = torch.empty((n, 4), dtype=torch.float32, device="cuda")
+        inst = torch.empty(n, dtype=torch.int32, device="cuda")
+        for any_hit in (False, True):
+            for _ in range(3):
+                soup.trace_device(d_rays.data_ptr(), n, hits.data_ptr(), inst.data_ptr(), any_hit=any_hit)
+            a.record()
+            for _ in range(5):
+                soup.trace_device(d_rays.data_ptr(), n, hits.data_ptr(), inst.data_ptr(), any_hit=any_hit)
+            b.record()
+            b.synchronize()
+            gms = a.elapsed_time(b) / 5
+            m = 1 << 18
+            t = time.perf_counter()
+            osc.trace(rays[:m], any_hit=any_hit, threads=threads)
+            cs = time.perf_counter() - t
+            res[f"{kind}_{'any' if any_hit else 'closest'}"] = {
+                "gpu_mrays_s": round(n / gms / 1e3, 1), "gpu_ms": round(gms, 3), "cpu_mrays_s": round(m / cs / 1e6, 2),
+                "ratio": round((n / gms / 1e3) / (m / cs / 1e6), 1)}
+        del d_rays, hits, inst
+    out["soup_1m_16m_rays"] = res
     return out
 
 
@@ -484,7 +574,10 @@ def run_reference(args):
 def main():
     args = parse()
     args.serving_loads = [(float(a), int(b)) for a, b in (x.split(":") for x in args.serving_loads.split(","))]
-    line = run_reference(args) if args.impl == "reference" else run_ours(args)
+    if args.all_configs:
+        line = configs_report(args)
+    else:
+        line = run_reference(args) if args.impl == "reference" else run_ours(args)
     if line is not None:
         print(json.dumps(line), flush=True)
 
