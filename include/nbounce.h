@@ -365,7 +365,10 @@ typedef struct nb_cache_config {
                                    with this decay per step (0.99); 0: the weights themselves */
   float grad_clip;              /* bound on |dloss/doutput| per record and channel (0: none);
                                    limits the pull of rare very bright targets (sun hits) */
+  uint32_t tensor_path;         /* cache lookups on NB_CACHE_TCGEN05 (default) or NB_CACHE_MMA_SYNC */
 } nb_cache_config;
+
+enum { NB_CACHE_TCGEN05 = 0, NB_CACHE_MMA_SYNC = 1 };
 
 /* One cache input before encoding (64 bytes). */
 typedef struct nb_cache_vertex {
@@ -400,7 +403,8 @@ int nb_cache_get_weights(const nb_cache* cache, float* weights, size_t n);
 int nb_cache_set_weights(nb_cache* cache, const float* weights, size_t n);
 /* The network's inputs of n vertices: device arrays, out is n x NB_CACHE_INPUTS floats. */
 int nb_cache_encode(nb_cache* cache, const nb_cache_vertex* vertices, size_t n, float* out, void* stream);
-/* Network outputs (n x 3) of encoded inputs (n x 64); device arrays, BF16 inside. */
+/* Network outputs (n x 3) of encoded inputs (n x 64); device arrays, BF16 inside.  With the
+ * tcgen05 path it synchronises stream (NB_ERR_TIMEOUT if a tensor-core wait gave up). */
 int nb_cache_infer(nb_cache* cache, const float* inputs, size_t n, float* out, void* stream);
 /* Mean gradient (NB_CACHE_PARAMS floats, device) and loss (host, may be NULL) of the relative
  * L2 loss sum((p - y)^2 / (p^2 + 0.01)) / (3 n), the denominator held constant; targets n x 3.

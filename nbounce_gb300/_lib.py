@@ -64,6 +64,8 @@ class NbKernelTimes(C.Structure):
 
 
 NB_CACHE_PARAMS = 21504
+NB_CACHE_TCGEN05 = 0
+NB_CACHE_MMA_SYNC = 1
 NB_CACHE_INPUTS = 64
 CACHE_VERTEX_DTYPE = np.dtype([("pos", "<f4", 3), ("roughness", "<f4"), ("wo", "<f4", 3), ("metallic", "<f4"),
                                ("n", "<f4", 3), ("tag", "<u4"), ("color", "<f4", 3), ("pad", "<f4")])
@@ -72,7 +74,8 @@ CACHE_VERTEX_DTYPE = np.dtype([("pos", "<f4", 3), ("roughness", "<f4"), ("wo", "
 class NbCacheConfig(C.Structure):
     _fields_ = [("learning_rate", C.c_float), ("beta1", C.c_float), ("beta2", C.c_float), ("epsilon", C.c_float),
                 ("spread", C.c_float), ("train_records", C.c_uint32), ("train_steps", C.c_uint32),
-                ("extra_vertices", C.c_uint32), ("seed", C.c_uint32), ("ema", C.c_float), ("grad_clip", C.c_float)]
+                ("extra_vertices", C.c_uint32), ("seed", C.c_uint32), ("ema", C.c_float), ("grad_clip", C.c_float),
+                ("tensor_path", C.c_uint32)]
 
 
 class NbCacheStats(C.Structure):

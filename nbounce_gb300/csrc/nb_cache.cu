@@ -10,8 +10,10 @@
 // Kernels (mma.sync m16n8k16, BF16 operands, FP32 accumulation; weights resident in shared
 // memory as 336 rows x 64 inputs, rows padded to 72 elements so that ldmatrix is
 // conflict-free):
-//   k_cache_infer_*  one warp evaluates 32 rows: the activations never leave registers
-//                    (the C fragment of layer l, ReLU'd and packed to BF16, is the A
+//   k_cache_infer_tc tcgen05.mma (5th-generation tensor cores): operands in shared memory,
+//                    FP32 accumulators in tensor memory, 4 groups of 128 rows per CTA
+//   k_cache_infer_*  mma.sync: one warp evaluates 32 rows, the activations never leave
+//                    registers (the C fragment of layer l, ReLU'd and packed to BF16, is the A
 //                    fragment of layer l + 1)
 //   k_cache_grad     one CTA of 8 warps takes 128 rows: forward with the activations kept in
 //                    shared memory, relative L2 loss (p - y)^2 / (p^2 + 0.01) with the
@@ -284,6 +286,281 @@ __global__ void __launch_bounds__(256, 2) k_cache_infer_queries(const bf16* __re
       }
     }
     __syncwarp();
+  }
+}
+
+// ---- inference on the 5th-generation tensor cores (tcgen05) ------------------------------
+//
+// A CTA is two warpgroups of 4 warps; each warpgroup keeps two groups of 128 rows in flight,
+// so an SM (2 CTAs) runs 8 independent layer chains and one chain's MMA round trip hides
+// behind the others' epilogues.  The MMA operands sit in shared memory in the no-swizzle
+// K-major canonical layout of tcgen05.mma: 8-row x 16-byte core matrices of 128 B, the core
+// matrices of one 8-row group along K contiguous (leading byte offset 128 B), 8-row groups
+// 1 KB apart (stride byte offset 1 KB).  Each group's accumulator (128 lanes x 64 FP32 columns)
+// lives in tensor memory.  Per layer and group the warpgroup's first thread issues four
+// K = 16 MMAs and commits them to the group's mbarrier; once they completed, the warps read
+// their 32 accumulator rows (tcgen05.ld), apply ReLU, pack to BF16 and overwrite the group's
+// operand with the next layer's (the MMA that read it is done).  The warp-collective
+// (.sync.aligned) tcgen05 instructions - alloc, ld, dealloc - run on whole converged warps.
+// Waits poll the mbarrier a bounded number of times: on a timeout the warpgroup raises
+// kStatusCacheTimeout (bits 16.. = 1 + the layer it waited for) and stops; the CTA frees its
+// TMEM before it exits.
+
+constexpr int kTcRows = 128;                                   // rows per group (= TMEM lanes)
+constexpr int kTcThreads = 256;                                // two warpgroups
+constexpr uint32_t kTcCols = 256;                              // TMEM columns: 64 per group, 4 groups
+constexpr uint32_t kTcLayerBytes = 8192;                       // one 64 x 64 layer, canonical
+constexpr size_t kTcWBytes = 5 * kTcLayerBytes + 2048;         // + the 16 x 64 output layer
+constexpr size_t kTcActBytes = (size_t)kTcRows * 64 * sizeof(bf16);  // 16 KB per group operand
+constexpr size_t kTcSmem = kTcWBytes + 4 * kTcActBytes;        // 108,544 B (2 CTAs per SM)
+constexpr uint32_t kTcWaitLimit = 1u << 22;                    // mbarrier polls per wait
+constexpr uint32_t kStatusCacheTimeout = 1u << 8;
+
+// byte offset of element (row, k) of a canonical K-major operand (rows x 64)
+__device__ __forceinline__ uint32_t canon_off(uint32_t row, uint32_t k) {
+  return (row >> 3) * 1024u + (k >> 3) * 128u + (row & 7u) * 16u + (k & 7u) * 2u;
+}
+
+// shared-memory matrix descriptor: start address, LBO 128 B, SBO 1024 B, descriptor version 1,
+// no swizzle
+__device__ __forceinline__ uint64_t tc_desc(uint32_t addr) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)(128u >> 4) << 16) | ((uint64_t)(1024u >> 4) << 32) |
+         (1ull << 46);
+}
+
+// instruction descriptor of kind::f16: FP32 accumulator, BF16 A and B, both K-major, M x N
+__host__ __device__ constexpr uint32_t tc_idesc(uint32_t M, uint32_t N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((N >> 3) << 17) | ((M >> 4) << 24);
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d_tmem, uint64_t a, uint64_t b, uint32_t idesc, uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\tsetp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}\n" ::"r"(d_tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+__device__ __forceinline__ void tc_commit(uint32_t mbar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];\n" ::"r"(mbar)
+               : "memory");
+}
+// polls (non-blocking test_wait) until the phase of the given parity completed
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+  for (uint32_t k = 0; k < kTcWaitLimit; ++k) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.test_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+        "selp.u32 %0, 1, 0, p;\n\t}\n"
+        : "=r"(done)
+        : "r"(mbar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+__device__ __forceinline__ void tc_fence_before() { asm volatile("tcgen05.fence::before_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void tc_fence_after() { asm volatile("tcgen05.fence::after_thread_sync;\n" ::: "memory"); }
+__device__ __forceinline__ void fence_async_smem() { asm volatile("fence.proxy.async.shared::cta;\n" ::: "memory"); }
+// barrier over the 128 threads of one warpgroup (named barrier 1 + wg); returns the OR of pred
+__device__ __forceinline__ bool wg_barrier_or(uint32_t wg, bool pred) {
+  uint32_t out;
+  asm volatile(
+      "{\n\t.reg .pred q, p;\n\tsetp.ne.u32 q, %1, 0;\n\tbar.red.or.pred p, %2, 128, q;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}\n"
+      : "=r"(out)
+      : "r"((uint32_t)pred), "r"(1u + wg)
+      : "memory");
+  return out != 0;
+}
+// 16 consecutive FP32 accumulator columns of this thread's TMEM lane
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
+  uint32_t r[16];
+  __syncwarp();  // warp-collective: lanes may leave the mbarrier poll at different times
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];\n\t"
+               "tcgen05.wait::ld.sync.aligned;\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+               : "r"(taddr)
+               : "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// kQueries: the rows are a wave's cache queries (encoded here; results go to radiance / tail);
+// else rows of encoded inputs X (bf16 [n][64]) with results in out[n][3].
+template <bool kQueries>
+__global__ void __launch_bounds__(kTcThreads, 2) k_cache_infer_tc(const bf16* __restrict__ W,
+                                                                  const bf16* __restrict__ X,
+                                                                  const CacheQuery* __restrict__ queries,
+                                                                  const uint32_t* __restrict__ n_dev, uint32_t n_host,
+                                                                  CacheBounds bounds, float* __restrict__ out,
+                                                                  float4* __restrict__ radiance,
+                                                                  float4* __restrict__ tail,
+                                                                  uint32_t* __restrict__ status) {
+  extern __shared__ __align__(128) unsigned char smem_tc[];
+  __shared__ __align__(8) uint64_t mbar_slot[4];
+  __shared__ uint32_t tmem_slot;
+  unsigned char* Wc = smem_tc;
+  const uint32_t warp = threadIdx.x >> 5, wg = threadIdx.x >> 7, tid = threadIdx.x & 127u;
+  // group j of warpgroup wg: operand at act + j * kTcActBytes, mbarrier mbar + 8 j, accumulator
+  // columns 128 wg + 64 j
+  unsigned char* act = smem_tc + kTcWBytes + 2u * wg * kTcActBytes;
+  const uint32_t mbar = saddr(&mbar_slot[2 * wg]);
+  const uint32_t n = kQueries ? min(*n_dev, n_host) : n_host;
+
+  // weights into the canonical layout: row r of layer l = global row 64 l + r
+  for (uint32_t i = threadIdx.x; i < (uint32_t)kMlpRows * 8u; i += blockDim.x) {
+    const uint32_t row = i >> 3, c = i & 7u, l = row >> 6, r = row & 63u;
+    *reinterpret_cast<uint4*>(Wc + l * kTcLayerBytes + canon_off(r, 8u * c)) =
+        __ldg(reinterpret_cast<const uint4*>(W) + i);
+  }
+  if (threadIdx.x == 0) {
+    for (uint32_t k = 0; k < 4; ++k)
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(saddr(&mbar_slot[k])) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    __syncwarp();  // alloc is .sync.aligned: the whole warp, converged
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(&tmem_slot)),
+                 "r"(kTcCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tmem_slot + 128u * wg;            // this warpgroup's two accumulators
+  const uint32_t lane_base = (32u * (warp & 3u)) << 16;  // this warp's 32 TMEM lanes
+  uint32_t phase[2] = {0u, 0u};
+  uint32_t fail_layer = 0;
+  bool failed = false;
+
+  // layer l of group j: four K = 16 MMAs into the group's 64 accumulator columns
+  auto issue = [&](uint32_t j, int l) {
+    const uint32_t a_base = saddr(act + j * kTcActBytes);
+    const uint32_t b_base = saddr(Wc + l * kTcLayerBytes);
+    const uint32_t idesc = tc_idesc(kTcRows, l < 5 ? 64u : 16u);
+#pragma unroll
+    for (uint32_t k = 0; k < 4; ++k)
+      tc_mma(tmem + 64u * j, tc_desc(a_base + 256u * k), tc_desc(b_base + 256u * k), idesc, k);
+    tc_commit(mbar + 8u * j);
+  };
+
+  const uint32_t groups = (n + kTcRows - 1) / kTcRows;
+  // round q covers row groups 4 q .. 4 q + 3 (warpgroup wg takes 4 q + 2 wg + j); rounds are
+  // dealt to the CTAs round-robin
+  for (uint32_t q = blockIdx.x; 4u * q + 2u * wg < groups && !failed; q += gridDim.x) {
+    uint32_t tag[2] = {0u, 0u};
+    float4 T[2];
+    V3 fac[2];
+#pragma unroll
+    for (uint32_t j = 0; j < 2; ++j) {
+      const uint32_t row = (4u * q + 2u * wg + j) * kTcRows + tid;
+      T[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+      fac[j] = V3{0.0f, 0.0f, 0.0f};
+      uint4 ch[8];
+      if (row < n) {
+        if (kQueries) {
+          const CacheQuery qr = queries[row];
+          tag[j] = qr.f.tag;
+          T[j] = qr.T;
+          fac[j] = cache_factor(qr.f);
+          float f[64];
+          cache_encode(qr.f, bounds, f);
+#pragma unroll
+          for (int c = 0; c < 8; ++c)
+            ch[c] = make_uint4(pack2(f[8 * c], f[8 * c + 1]), pack2(f[8 * c + 2], f[8 * c + 3]),
+                               pack2(f[8 * c + 4], f[8 * c + 5]), pack2(f[8 * c + 6], f[8 * c + 7]));
+        } else {
+#pragma unroll
+          for (int c = 0; c < 8; ++c) ch[c] = __ldg(reinterpret_cast<const uint4*>(X + (size_t)row * 64) + c);
+        }
+      } else {
+#pragma unroll
+        for (int c = 0; c < 8; ++c) ch[c] = make_uint4(0u, 0u, 0u, 0u);
+      }
+      unsigned char* a = act + j * kTcActBytes;
+#pragma unroll
+      for (int c = 0; c < 8; ++c) *reinterpret_cast<uint4*>(a + canon_off(tid, 8u * c)) = ch[c];
+    }
+    fence_async_smem();
+    tc_fence_before();
+    wg_barrier_or(wg, false);
+    tc_fence_after();
+    if (tid == 0) {
+      issue(0, 0);
+      issue(1, 0);
+    }
+#pragma unroll 1
+    for (int l = 0; l < 6 && !failed; ++l) {
+#pragma unroll
+      for (uint32_t j = 0; j < 2; ++j) {
+        const bool ok = mbar_wait(mbar + 8u * j, phase[j]);
+        phase[j] ^= 1u;
+        tc_fence_after();
+        const uint32_t t_row = tmem + 64u * j + lane_base;
+        if (l < 5) {
+          unsigned char* a = act + j * kTcActBytes;  // its MMA is complete: overwrite in place
+#pragma unroll
+          for (int c4 = 0; c4 < 4; ++c4) {
+            float v[16];
+            tc_ld16(t_row + 16u * c4, v);
+            *reinterpret_cast<uint4*>(a + canon_off(tid, 16u * c4)) =
+                make_uint4(pack2(relu(v[0]), relu(v[1])), pack2(relu(v[2]), relu(v[3])),
+                           pack2(relu(v[4]), relu(v[5])), pack2(relu(v[6]), relu(v[7])));
+            *reinterpret_cast<uint4*>(a + canon_off(tid, 16u * c4 + 8u)) =
+                make_uint4(pack2(relu(v[8]), relu(v[9])), pack2(relu(v[10]), relu(v[11])),
+                           pack2(relu(v[12]), relu(v[13])), pack2(relu(v[14]), relu(v[15])));
+          }
+          fence_async_smem();
+        } else {
+          // every lane of every warp runs the (warp-collective) accumulator load; only rows
+          // of the batch use it
+          float v[16];
+          tc_ld16(t_row, v);
+          const uint32_t row = (4u * q + 2u * wg + j) * kTcRows + tid;
+          if (!ok || row >= n) {
+          } else if (kQueries) {
+            const V3 L{fmaxf(v[0], 0.0f) * fac[j].x, fmaxf(v[1], 0.0f) * fac[j].y, fmaxf(v[2], 0.0f) * fac[j].z};
+            if (tag[j] & nb::kCacheTailBit) {
+              tail[tag[j] & ~nb::kCacheTailBit] = make_float4(L.x, L.y, L.z, 0.0f);
+            } else {
+              float4 c = radiance[tag[j]];
+              c.x = c.x + T[j].x * L.x;
+              c.y = c.y + T[j].y * L.y;
+              c.z = c.z + T[j].z * L.z;
+              radiance[tag[j]] = c;
+            }
+          } else {
+            out[3 * (size_t)row] = v[0];
+            out[3 * (size_t)row + 1] = v[1];
+            out[3 * (size_t)row + 2] = v[2];
+          }
+        }
+        tc_fence_before();
+        failed = wg_barrier_or(wg, !ok);
+        tc_fence_after();
+        if (failed) {
+          fail_layer = (uint32_t)l + 1u;
+          break;
+        }
+        if (l < 5 && tid == 0) issue(j, l + 1);
+      }
+    }
+  }
+  if (failed && tid == 0) {
+    atomicOr(status, kStatusCacheTimeout | (fail_layer << 16));
+    // give outstanding MMAs a bounded chance to finish before the memory is released
+    mbar_wait(mbar, phase[0] ^ 1u);
+    mbar_wait(mbar + 8u, phase[1] ^ 1u);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    __syncwarp();  // dealloc is .sync.aligned
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem_slot), "r"(kTcCols)
+                 : "memory");
   }
 }
 
@@ -663,6 +940,7 @@ struct nb_cache {
   nbd::bf16* web = nullptr;
   float* m = nullptr;
   float* v = nullptr;
+  uint32_t* status = nullptr;  // tensor-core wait timeouts of nb_cache_infer
   float* part_dw = nullptr;
   float* part_loss = nullptr;
   uint32_t part_cap = 0;  // CTAs the partial buffers hold
@@ -717,6 +995,12 @@ int set_smem_limits() {
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(nbd::k_cache_infer_queries, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)nbd::kInferSmem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(nbd::k_cache_infer_tc<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)nbd::kTcSmem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(nbd::k_cache_infer_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)nbd::kTcSmem);
     rc = e == cudaSuccess ? NB_OK : cuda_fail(e, "cudaFuncSetAttribute(cache kernels)");
   });
   return rc;
@@ -902,10 +1186,15 @@ int cache_wave_begin(nb_cache* c, const nb_scene* scene, uint32_t n_paths, Cache
 
 // After the last bounce: cache lookups of the wave's queries.
 int cache_wave_infer(nb_cache* c, const PathBatch& pb, int sms, cudaStream_t st) {
-  nbd::k_cache_infer_queries<<<2 * sms, 256, nbd::kInferSmem, st>>>(c->cfg.ema > 0.0f ? c->web : c->wb, c->queries,
-                                                                    c->counters,
-                                                                    c->cap_paths + c->cap_slots, c->bounds,
-                                                                    pb.radiance, c->tail);
+  const nbd::bf16* w = c->cfg.ema > 0.0f ? c->web : c->wb;
+  if (c->cfg.tensor_path == NB_CACHE_TCGEN05)
+    nbd::k_cache_infer_tc<true><<<2 * sms, nbd::kTcThreads, nbd::kTcSmem, st>>>(
+        w, nullptr, c->queries, c->counters, c->cap_paths + c->cap_slots, c->bounds, nullptr, pb.radiance, c->tail,
+        pb.status);
+  else
+    nbd::k_cache_infer_queries<<<2 * sms, 256, nbd::kInferSmem, st>>>(w, c->queries, c->counters,
+                                                                      c->cap_paths + c->cap_slots, c->bounds,
+                                                                      pb.radiance, c->tail);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "cache lookup launch");
   return NB_OK;
@@ -951,6 +1240,7 @@ void nb_cache_default_config(nb_cache_config* cfg) {
   cfg->seed = 0x5EED0u;
   cfg->ema = 0.99f;
   cfg->grad_clip = 0.0f;
+  cfg->tensor_path = NB_CACHE_TCGEN05;
 }
 
 int nb_cache_create(const nb_cache_config* cfg, nb_cache** out) {
@@ -967,12 +1257,14 @@ int nb_cache_create(const nb_cache_config* cfg, nb_cache** out) {
   if (c.extra_vertices > nb::kCacheMaxVertices) return fail(NB_ERR_INVALID_ARG, "extra_vertices must be <= 8");
   if (!(c.ema >= 0.0f && c.ema < 1.0f) || !(c.grad_clip >= 0.0f))
     return fail(NB_ERR_INVALID_ARG, "ema must be in [0, 1) and grad_clip >= 0");
+  if (c.tensor_path != NB_CACHE_TCGEN05 && c.tensor_path != NB_CACHE_MMA_SYNC)
+    return fail(NB_ERR_INVALID_ARG, "unknown tensor_path");
   int n_dev = 0;
   if (cudaGetDeviceCount(&n_dev) != cudaSuccess || n_dev == 0) return fail(NB_ERR_NO_DEVICE, "no CUDA device");
   nb_cache* h = new (std::nothrow) nb_cache();
   if (!h) return fail(NB_ERR_OOM, "host allocation failed");
   h->cfg = c;
-  void* p[6] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
+  void* p[7] = {nullptr, nullptr, nullptr, nullptr, nullptr, nullptr, nullptr};
   int rc = NB_OK;
   for (int k = 0; k < 6 && !rc; ++k)
     rc = h->arena.alloc(kMlpParams * ((k == 1 || k == 3) ? sizeof(nbd::bf16) : sizeof(float)), &p[k]);
@@ -982,6 +1274,8 @@ int nb_cache_create(const nb_cache_config* cfg, nb_cache** out) {
   h->web = (nbd::bf16*)p[3];
   h->m = (float*)p[4];
   h->v = (float*)p[5];
+  if (!rc) rc = h->arena.alloc(sizeof(uint32_t), &p[6]);
+  h->status = (uint32_t*)p[6];
   if (!rc) {
     // He-uniform initialisation: U(-sqrt(6 / 64), sqrt(6 / 64)); padding rows of W_5 zero
     std::vector<float> w(kMlpParams, 0.0f);
@@ -1065,9 +1359,24 @@ int nb_cache_infer(nb_cache* c, const float* enc, size_t n, float* out, void* st
   cudaStream_t st = (cudaStream_t)stream;
   const int sms = sm_count();
   nbd::k_to_bf16<<<grid_for(n * 64, 256, sms), 256, 0, st>>>(enc, c->sx, n * 64);
-  nbd::k_cache_infer_rows<<<std::min<size_t>((n + 255) / 256, 2 * (size_t)sms), 256, nbd::kInferSmem, st>>>(
-      c->wb, c->sx, (uint32_t)n, out);
+  if (c->cfg.tensor_path == NB_CACHE_TCGEN05) {
+    NB_CUDA(cudaMemsetAsync(c->status, 0, sizeof(uint32_t), st), "cudaMemsetAsync");
+    const size_t rounds = (n + 4 * nbd::kTcRows - 1) / (4 * nbd::kTcRows);
+    nbd::k_cache_infer_tc<false><<<(unsigned)std::min<size_t>(rounds, 2 * (size_t)sms), nbd::kTcThreads,
+                                   nbd::kTcSmem, st>>>(c->wb, c->sx, nullptr, nullptr, (uint32_t)n, c->bounds, out,
+                                                       nullptr, nullptr, c->status);
+  } else {
+    nbd::k_cache_infer_rows<<<std::min<size_t>((n + 255) / 256, 2 * (size_t)sms), 256, nbd::kInferSmem, st>>>(
+        c->wb, c->sx, (uint32_t)n, out);
+  }
   NB_CUDA(cudaGetLastError(), "cache infer launch");
+  if (c->cfg.tensor_path == NB_CACHE_TCGEN05) {
+    uint32_t status = 0;
+    NB_CUDA(cudaMemcpyAsync(&status, c->status, sizeof(status), cudaMemcpyDeviceToHost, st), "cudaMemcpyAsync");
+    NB_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    if (status & nbd::kStatusCacheTimeout)
+      return fail(NB_ERR_TIMEOUT, "tensor-core wait timed out (layer %u)", (status >> 16) - 1u);
+  }
   return NB_OK;
 }
 

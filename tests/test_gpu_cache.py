@@ -49,8 +49,11 @@ def dev(a):
     return torch.from_numpy(np.ascontiguousarray(a)).cuda()
 
 
-def test_infer_matches_reference():
-    c = RadianceCache(seed=7)
+@pytest.mark.parametrize("path", [L.NB_CACHE_TCGEN05, L.NB_CACHE_MMA_SYNC])
+def test_infer_matches_reference(path):
+    """Both tensor-core paths (tcgen05 with tensor-memory accumulators, and mma.sync) against
+    the emulated-BF16 reference, on a row count that is not a multiple of 128."""
+    c = RadianceCache(seed=7, tensor_path=path)
     w = c.get_weights()
     x, _ = batch(1000, 1)
     out = torch.zeros(1000, 3, device="cuda")
