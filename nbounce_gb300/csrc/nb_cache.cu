@@ -22,7 +22,7 @@
 //                    as a per-CTA FP32 partial (no atomics)
 //   k_cache_adam     sums the partials in CTA order (deterministic), Adam update of the FP32
 //                    master weights and of their BF16 copy
-//   k_cache_scan / k_cache_gather  turn the training paths' vertex chains into records:
+//   k_cache_count / _offsets / _gather  turn the training paths' vertex chains into records:
 //                    radiance targets by a backward walk over the throughput factors, encoded
 //                    inputs, reflectance-factorised targets; adapt the training-path density
 //                    to the record budget
@@ -820,21 +820,19 @@ __global__ void __launch_bounds__(256) k_cache_adam(float* __restrict__ w, bf16*
 
 // ---- training records --------------------------------------------------------------------
 
-// counters: [0] queries, [1] records found, [2] records used, [3] slots of the wave
-// Single CTA: exclusive scan of the per-slot vertex counts, record budget, next stride.
-__global__ void __launch_bounds__(1024) k_cache_scan(const uint32_t* __restrict__ vert_count, uint32_t max_slots,
-                                                     uint32_t n_paths, uint32_t budget, uint32_t* stride,
-                                                     uint32_t* __restrict__ offsets, uint32_t* counters) {
-  __shared__ uint32_t warp_sums[32];
-  const uint32_t G = *stride;
-  const uint32_t n_slots = min(max_slots, (n_paths + G - 1) / G);
-  const uint32_t per = (n_slots + blockDim.x - 1) / blockDim.x;
-  const uint32_t b = threadIdx.x * per, e = min(b + per, n_slots);
-  uint32_t local = 0;
-  for (uint32_t s = b; s < e; ++s) local += vert_count[s];
-  // block exclusive scan of `local`
+// counters: [0] queries, [1] records found, [2] records used, [3] slots of the wave.
+// The exclusive scan of the per-slot vertex counts runs in two passes over tiles of
+// kScanTile slots (one tile per block): block sums, then each tile's scan plus the sum of the
+// tiles before it.  The order of the records is fixed by the slots, so training stays
+// deterministic.
+constexpr int kScanThreads = 512;
+constexpr int kScanPer = 8;
+constexpr int kScanTile = kScanThreads * kScanPer;  // 4096 slots per block
+
+// exclusive scan of one value per thread over a kScanThreads block; *total = block sum
+__device__ __forceinline__ uint32_t block_exclusive_scan(uint32_t v, uint32_t* warp_sums, uint32_t* total) {
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  uint32_t incl = local;
+  uint32_t incl = v;
 #pragma unroll
   for (int d = 1; d < 32; d <<= 1) {
     const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, incl, d);
@@ -843,7 +841,7 @@ __global__ void __launch_bounds__(1024) k_cache_scan(const uint32_t* __restrict_
   if (lane == 31) warp_sums[warp] = incl;
   __syncthreads();
   if (warp == 0) {
-    uint32_t ws = lane < (int)(blockDim.x >> 5) ? warp_sums[lane] : 0u;
+    uint32_t ws = lane < kScanThreads / 32 ? warp_sums[lane] : 0u;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const uint32_t y = __shfl_up_sync(0xFFFFFFFFu, ws, d);
@@ -852,19 +850,79 @@ __global__ void __launch_bounds__(1024) k_cache_scan(const uint32_t* __restrict_
     warp_sums[lane] = ws;  // inclusive over warps
   }
   __syncthreads();
-  uint32_t run = incl - local + (warp > 0 ? warp_sums[warp - 1] : 0u);
-  for (uint32_t s = b; s < e; ++s) {
-    offsets[s] = run;
-    run += vert_count[s];
+  *total = warp_sums[kScanThreads / 32 - 1];
+  return incl - v + (warp > 0 ? warp_sums[warp - 1] : 0u);
+}
+
+// Pass 1: the wave's slot count (from the stride its shade kernels used) and each tile's sum.
+__global__ void __launch_bounds__(kScanThreads) k_cache_count(const uint32_t* __restrict__ vert_count,
+                                                              uint32_t max_slots, uint32_t n_paths,
+                                                              const uint32_t* __restrict__ stride,
+                                                              uint32_t* __restrict__ block_sums,
+                                                              uint32_t* __restrict__ counters) {
+  __shared__ uint32_t warp_sums[32];
+  const uint32_t G = *stride;
+  const uint32_t n_slots = min(max_slots, (n_paths + G - 1) / G);
+  if (blockIdx.x == 0 && threadIdx.x == 0) counters[3] = n_slots;
+  const uint32_t base = blockIdx.x * (uint32_t)kScanTile;
+  uint32_t sum = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    const uint32_t i = base + (uint32_t)k * kScanThreads + threadIdx.x;
+    if (i < n_slots) sum += vert_count[i];
   }
-  if (threadIdx.x == blockDim.x - 1) {
-    const uint32_t total = run;
-    counters[1] = total;
-    counters[2] = min(total, budget);
-    counters[3] = n_slots;
-    // one training path per G paths gives `total` records: aim the next wave at the budget
+  uint32_t total;
+  block_exclusive_scan(sum, warp_sums, &total);
+  if (threadIdx.x == 0) block_sums[blockIdx.x] = total;
+}
+
+// Pass 2: each slot's first record, the record totals and the next wave's stride.
+__global__ void __launch_bounds__(kScanThreads) k_cache_offsets(const uint32_t* __restrict__ vert_count,
+                                                                const uint32_t* __restrict__ block_sums,
+                                                                uint32_t n_blocks, uint32_t max_slots,
+                                                                uint32_t n_paths, uint32_t budget, uint32_t* stride,
+                                                                uint32_t* __restrict__ offsets, uint32_t* counters) {
+  __shared__ uint32_t warp_sums[32];
+  __shared__ uint32_t tile[kScanTile];
+  __shared__ uint32_t prefix;
+  const uint32_t n_slots = counters[3];
+  const uint32_t base = blockIdx.x * (uint32_t)kScanTile;
+  if (threadIdx.x == 0) {
+    uint32_t p = 0;
+    for (uint32_t b = 0; b < blockIdx.x; ++b) p += block_sums[b];
+    prefix = p;
+  }
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    const uint32_t j = (uint32_t)k * kScanThreads + threadIdx.x, i = base + j;
+    tile[j] = i < n_slots ? vert_count[i] : 0u;
+  }
+  __syncthreads();
+  uint32_t local[kScanPer], sum = 0;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    local[k] = sum;
+    sum += tile[threadIdx.x * kScanPer + k];
+  }
+  uint32_t total;
+  const uint32_t before = block_exclusive_scan(sum, warp_sums, &total) + prefix;
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) tile[threadIdx.x * kScanPer + k] = before + local[k];
+  __syncthreads();
+#pragma unroll
+  for (int k = 0; k < kScanPer; ++k) {
+    const uint32_t j = (uint32_t)k * kScanThreads + threadIdx.x, i = base + j;
+    if (i < n_slots) offsets[i] = tile[j];
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    uint32_t all = 0;
+    for (uint32_t b = 0; b < n_blocks; ++b) all += block_sums[b];
+    counters[1] = all;
+    counters[2] = min(all, budget);
+    // one training path per G paths gave `all` records: aim the next wave at the budget
+    const uint32_t G = *stride;
     const uint32_t g_min = max(1u, (n_paths + max_slots - 1) / max_slots);
-    double next = total ? (double)G * (double)total / (double)budget : (double)g_min;
+    double next = all ? (double)G * (double)all / (double)budget : (double)g_min;
     next = fmin(fmax(next, (double)g_min), (double)nb::kCacheMaxStride);
     *stride = (uint32_t)(next + 0.5);
   }
@@ -959,6 +1017,7 @@ struct nb_cache {
   uint32_t* vert_count = nullptr;
   float4* tail = nullptr;
   uint32_t* offsets = nullptr;
+  uint32_t* block_sums = nullptr;  // per scan tile
   uint32_t* stride = nullptr;
   nbd::bf16* X = nullptr;
   float4* Y = nullptr;
@@ -1141,6 +1200,8 @@ int cache_wave_begin(nb_cache* c, const nb_scene* scene, uint32_t n_paths, Cache
     c->tail = (float4*)p;
     if ((rc = c->wave.alloc((size_t)S * sizeof(uint32_t), &p))) return rc;
     c->offsets = (uint32_t*)p;
+    if ((rc = c->wave.alloc(((size_t)S + nbd::kScanTile - 1) / nbd::kScanTile * sizeof(uint32_t), &p))) return rc;
+    c->block_sums = (uint32_t*)p;
     if ((rc = c->wave.alloc(sizeof(uint32_t), &p))) return rc;
     c->stride = (uint32_t*)p;
     if ((rc = c->wave.alloc((size_t)R * 64 * sizeof(nbd::bf16), &p))) return rc;
@@ -1202,9 +1263,16 @@ int cache_wave_infer(nb_cache* c, const PathBatch& pb, int sms, cudaStream_t st)
 
 // Then: training records from the training paths' chains and the optimiser steps.
 int cache_wave_train(nb_cache* c, uint32_t n_paths, int sms, cudaStream_t st) {
-  nbd::k_cache_scan<<<1, 1024, 0, st>>>(c->vert_count, c->cap_slots, n_paths, c->cfg.train_records, c->stride,
-                                        c->offsets, c->counters);
+  const uint32_t tiles = (c->cap_slots + nbd::kScanTile - 1) / nbd::kScanTile;
+  nbd::k_cache_count<<<tiles, nbd::kScanThreads, 0, st>>>(c->vert_count, c->cap_slots, n_paths, c->stride,
+                                                          c->block_sums, c->counters);
   cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    nbd::k_cache_offsets<<<tiles, nbd::kScanThreads, 0, st>>>(c->vert_count, c->block_sums, tiles, c->cap_slots,
+                                                              n_paths, c->cfg.train_records, c->stride, c->offsets,
+                                                              c->counters);
+    e = cudaGetLastError();
+  }
   if (e == cudaSuccess) {
     nbd::k_cache_gather<<<grid_for(c->cap_slots, 128, sms), 128, 0, st>>>(
         c->verts, c->vert_count, c->tail, c->offsets, c->counters, c->bounds, c->X, c->Y);
