@@ -407,11 +407,13 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_cache_infer_tc(const bf16* __
   const uint32_t mbar = saddr(&mbar_slot[2 * wg]);
   const uint32_t n = kQueries ? min(*n_dev, n_host) : n_host;
 
-  // weights into the canonical layout: row r of layer l = global row 64 l + r
+  // weights into the canonical layout: row r of layer l = global row 64 l + r.  Consecutive
+  // threads take consecutive rows of one 16-byte column chunk, so each quarter-warp stores 128
+  // contiguous bytes (a thread per chunk of one row would hit one bank group 8 times)
   for (uint32_t i = threadIdx.x; i < (uint32_t)kMlpRows * 8u; i += blockDim.x) {
-    const uint32_t row = i >> 3, c = i & 7u, l = row >> 6, r = row & 63u;
+    const uint32_t row = i % (uint32_t)kMlpRows, c = i / (uint32_t)kMlpRows, l = row >> 6, r = row & 63u;
     *reinterpret_cast<uint4*>(Wc + l * kTcLayerBytes + canon_off(r, 8u * c)) =
-        __ldg(reinterpret_cast<const uint4*>(W) + i);
+        __ldg(reinterpret_cast<const uint4*>(W) + 8u * row + c);
   }
   if (threadIdx.x == 0) {
     for (uint32_t k = 0; k < 4; ++k)
@@ -798,8 +800,14 @@ __global__ void __launch_bounds__(256) k_cache_adam(float* __restrict__ w, bf16*
     *loss_out = s * scale;
   }
   if (p >= (uint32_t)kMlpParams) return;
-  float gsum = 0.0f;
-  for (uint32_t c = 0; c < parts; ++c) gsum += part_dw[(size_t)c * kMlpParams + p];
+  // eight independent partial sums keep eight loads in flight; combined in a fixed order
+  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+  uint32_t c = 0;
+  for (; c + 8 <= parts; c += 8)
+#pragma unroll
+    for (int k = 0; k < 8; ++k) acc[k] += part_dw[(size_t)(c + k) * kMlpParams + p];
+  for (; c < parts; ++c) acc[c & 7u] += part_dw[(size_t)c * kMlpParams + p];
+  const float gsum = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
   const bool live = p < kLiveEnd;
   const float gr = live ? gsum * scale : 0.0f;
   if (grad_out) grad_out[p] = gr;

@@ -213,7 +213,7 @@ def test_trained_cache_beats_plain_at_equal_samples(room, spread, min_gain):
     after 200 one-sample frames of online training, cache mode at 4 spp against plain 4 spp,
     both scored by relMSE against a 4096-spp plain render.  spread 0.01 ends paths by the
     spread rule (typically after one diffuse bounce); spread < 0 queries at the primary hit.
-    Training is deterministic, so the measured gains (1.9x and 11x) repeat exactly."""
+    Training is deterministic, so the measured gains (1.9x and 10.6x) repeat exactly."""
     desc, scene, env, cam, ref = room
     c = RadianceCache(seed=5, spread=spread, train_records=16384, train_steps=2)
     render(desc, scene, env, cam, 1, cache=c, frames=200)
