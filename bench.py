@@ -13,7 +13,8 @@ same 132.7M paths.  Mrays/s counts traversal queries (primary + extension rays).
   e2e    the same frames through the C ABI with host buffers: the camera struct goes in and
          the 33 MB RGBA32F image comes back to pinned host memory inside every step.
 
-The line also carries `quality` (relMSE of 16/64/256 spp against a 16,384-spp render),
+The line also carries `quality` (relMSE of 16/64/256 spp against a 16,384-spp render, plain
+and with environment next-event estimation),
 `serving` (render-job server p50/p99 under Poisson loads) and `cache` (the learned radiance
 cache: online training along a seeded camera spline, then relMSE and frame time of cache
 mode against plain 16/64 spp at the last camera, with the MLP kernels' tensor-core rate).
@@ -204,6 +205,12 @@ def quality_report(args, ref_spp=16384, width=480, height=270):
         pt.invalidate()
         pt.render(scene, cam, env, spp)
         out[f"relmse_{spp}spp"] = round(rel_mse(pt.download(), ref), 6)
+    # the same frames with environment next-event estimation (MIS), an opt-in estimator
+    pt.set_sampling(env_nee=True)
+    for spp in (16, 64, 256):
+        pt.invalidate()
+        pt.render(scene, cam, env, spp)
+        out[f"nee_relmse_{spp}spp"] = round(rel_mse(pt.download(), ref), 6)
     return out
 
 
@@ -283,6 +290,13 @@ def cache_report(args, desc, scene, env, stream):
         frame(plain, last, spp)
         ms = frame(plain, last, spp)
         out["plain"][f"{spp}spp"] = {"relmse": round(rel_mse(plain.download(stream=sh), ref), 5), "ms": round(ms, 2)}
+    # environment next-event estimation (no cache): the opt-in estimator aimed at the sun disc
+    out["nee"] = {}
+    plain.set_sampling(env_nee=True)
+    for spp in (4, 16, 64):
+        frame(plain, last, spp)
+        ms = frame(plain, last, spp)
+        out["nee"][f"{spp}spp"] = {"relmse": round(rel_mse(plain.download(stream=sh), ref), 5), "ms": round(ms, 2)}
     plain.close()
     peak = measured_peaks_all().get("bf16_tflops")
     for name, cfg in (("primary", dict(spread=-1.0)), ("spread", dict(spread=0.01))):

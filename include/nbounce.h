@@ -244,6 +244,22 @@ int nb_pathtracer_enable_timing(nb_pathtracer* pt, int enable);
 /* Sums the recorded launch times (synchronises stream); reset != 0 clears the record. */
 int nb_pathtracer_kernel_times(nb_pathtracer* pt, nb_kernel_times* out, int reset, void* stream);
 
+/* Estimator options.  0 (default) is the reference's: BSDF sampling only, the environment
+ * reached only by rays that escape.  NB_SAMPLE_ENV_NEE adds next-event estimation toward the
+ * environment (the reference's README lists environment importance sampling as planned work,
+ * README.md:20, pathtracing.wgsl:191 TODO): each non-emissive vertex also samples one
+ * direction from the environment's radiance distribution (luminance x sin(theta) per equirect
+ * texel; uniform for a constant environment) and traces a shadow ray; the two techniques are
+ * combined per BRDF lobe by the power heuristic, so the image converges to the same result
+ * with far less variance from small bright sources (a sun disc).  Ignored while a radiance
+ * cache is attached. */
+enum { NB_SAMPLE_ENV_NEE = 1u << 0 };
+int nb_pathtracer_set_sampling(nb_pathtracer* pt, uint32_t flags);
+int nb_pathtracer_get_sampling(const nb_pathtracer* pt, uint32_t* flags);
+/* Environment importance samples: for n uniform pairs u (device, 2n floats) writes n x
+ * (direction xyz, solid-angle density) to out (device, 4n floats).  Stream-ordered. */
+int nb_env_sample(const nb_env* env, const float* u, size_t n, float* out, void* stream);
+
 /* ---------------------------------------------------------------------------------------
  * Traversal (the intersect_scene query, raytracing_sw.wgsl:138-250, on caller rays)
  * ------------------------------------------------------------------------------------- */

@@ -25,6 +25,7 @@ NB_ENV_CONSTANT = 0
 NB_ENV_EQUIRECT = 1
 NB_TRACE_CLOSEST = 0
 NB_TRACE_ANY = 1
+NB_SAMPLE_ENV_NEE = 1
 
 VERTEX_DTYPE = np.dtype([("pos", "<f4", 3), ("u", "<f4"), ("nrm", "<f4", 3), ("v", "<f4"), ("tan", "<f4", 4)])
 NODE_DTYPE = np.dtype([("min", "<f4", 3), ("start", "<u4"), ("max", "<f4", 3), ("end", "<u4")])
@@ -175,6 +176,9 @@ def lib():
         "nb_cache_train_step": ([vp, vp, vp, sz, vp, vp], i32),
         "nb_cache_get_stats": ([vp, vp, vp], i32),
         "nb_pathtracer_set_cache": ([vp, vp], i32),
+        "nb_pathtracer_set_sampling": ([vp, u32], i32),
+        "nb_pathtracer_get_sampling": ([vp, vp], i32),
+        "nb_env_sample": ([vp, vp, sz, vp, vp], i32),
     }
     for name, (args, res) in sig.items():
         f = getattr(L, name)

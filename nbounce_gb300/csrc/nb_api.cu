@@ -6,6 +6,7 @@
 // owns every device allocation; failures return a status and set a thread-local message.
 
 #include <algorithm>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -57,6 +58,10 @@ struct nb_pathtracer {
   uint32_t capacity = 0;  // paths the work buffers hold
   uint32_t batch_paths = 1u << 27;
   nb_cache* cache = nullptr;  // radiance-cache mode when set
+  uint32_t sampling = 0;      // NB_SAMPLE_* flags
+  DeviceArena shadow;         // shadow-ray queue of environment next-event estimation
+  uint32_t shadow_capacity = 0;
+  ShadowQueue sq{};
   int sms = 1;
   // optional per-kernel event timing: (kind, start, stop) of every recorded launch
   bool timing = false;
@@ -274,6 +279,59 @@ void nb_scene_destroy(nb_scene* s) {
 }
 
 // ---- environment -----------------------------------------------------------------------
+// Importance-sampling tables of an equirect map: texel weight w = luminance x sin(theta) of
+// the texel row's centre (the solid angle of a texel is proportional to sin(theta)), negative
+// or non-finite luminance counted as 0, a uniform weight if the whole map is black.  Sums in
+// double, tables in float: marginal CDF over rows, a CDF per row, and per texel the density
+// over (u, v) = w / sum(w) x width x height.
+static int build_env_distribution(nb_env* e, const nb_env_desc* desc) {
+  const uint32_t W = desc->width, H = desc->height;
+  std::vector<double> w((size_t)W * H), row_sum(H, 0.0);
+  double total = 0.0;
+  for (int pass = 0; pass < 2 && !(total > 0.0); ++pass) {
+    total = 0.0;
+    for (uint32_t y = 0; y < H; ++y) {
+      const double sin_t = std::sin(3.14159265358979323846 * ((double)y + 0.5) / (double)H);
+      double r = 0.0;
+      for (uint32_t x = 0; x < W; ++x) {
+        const float* t = desc->texels + ((size_t)y * W + x) * 4;
+        double lum = pass == 0 ? 0.2126 * t[0] + 0.7152 * t[1] + 0.0722 * t[2] : 1.0;
+        if (!(lum > 0.0) || !std::isfinite(lum)) lum = 0.0;
+        w[(size_t)y * W + x] = lum * sin_t;
+        r += lum * sin_t;
+      }
+      row_sum[y] = r;
+      total += r;
+    }
+  }
+  std::vector<float> cdf_rows(H + 1), cdf_cols((size_t)H * (W + 1)), pdf_uv((size_t)W * H);
+  double acc = 0.0;
+  cdf_rows[0] = 0.0f;
+  for (uint32_t y = 0; y < H; ++y) {
+    acc += row_sum[y];
+    cdf_rows[y + 1] = (float)(acc / total);
+    float* c = cdf_cols.data() + (size_t)y * (W + 1);
+    double a = 0.0;
+    c[0] = 0.0f;
+    for (uint32_t x = 0; x < W; ++x) {
+      a += w[(size_t)y * W + x];
+      c[x + 1] = row_sum[y] > 0.0 ? (float)(a / row_sum[y]) : (float)(x + 1) / (float)W;
+      pdf_uv[(size_t)y * W + x] = (float)(w[(size_t)y * W + x] / total * (double)W * (double)H);
+    }
+    c[W] = 1.0f;
+  }
+  cdf_rows[H] = 1.0f;
+  const float *cr = nullptr, *cc = nullptr, *pu = nullptr;
+  int st;
+  if ((st = e->arena.upload(cdf_rows, &cr)) || (st = e->arena.upload(cdf_cols, &cc)) ||
+      (st = e->arena.upload(pdf_uv, &pu)))
+    return st;
+  e->dev.cdf_rows = cr;
+  e->dev.cdf_cols = cc;
+  e->dev.pdf_uv = pu;
+  return NB_OK;
+}
+
 int nb_env_create(const nb_env_desc* desc, nb_env** out) {
   if (!desc || !out) return fail(NB_ERR_INVALID_ARG, "NULL argument");
   *out = nullptr;
@@ -300,6 +358,11 @@ int nb_env_create(const nb_env_desc* desc, nb_env** out) {
     e->dev.texels = (const float4*)p;
     e->dev.width = desc->width;
     e->dev.height = desc->height;
+    if ((st = build_env_distribution(e, desc))) {
+      e->arena.release();
+      delete e;
+      return st;
+    }
   }
   *out = e;
   return NB_OK;
@@ -388,6 +451,7 @@ void nb_pathtracer_destroy(nb_pathtracer* pt) {
   pt->work.release();
   pt->tables.release();
   pt->image.release();
+  pt->shadow.release();
   delete pt;
 }
 
@@ -412,6 +476,28 @@ static int ensure_capacity(nb_pathtracer* pt, uint32_t paths) {
   b.radiance = f4[7];
   b.hit_inst = (uint32_t*)p;
   pt->capacity = paths;
+  return NB_OK;
+}
+
+// shadow-ray queue for `paths` paths (one ray per path and bounce at most) + its counters
+static int ensure_shadow(nb_pathtracer* pt, uint32_t paths) {
+  if (pt->shadow_capacity >= paths) return NB_OK;
+  pt->shadow.release();
+  pt->shadow_capacity = 0;
+  void* p[4] = {nullptr, nullptr, nullptr, nullptr};
+  int st = NB_OK;
+  for (int k = 0; k < 3 && !st; ++k) st = pt->shadow.alloc((size_t)paths * sizeof(float4), &p[k]);
+  if (!st) st = pt->shadow.alloc(2 * kMaxBounceSlots * sizeof(uint32_t), &p[3]);
+  if (st) {
+    pt->shadow.release();
+    return st;
+  }
+  pt->sq.o = (float4*)p[0];
+  pt->sq.d = (float4*)p[1];
+  pt->sq.c = (float4*)p[2];
+  pt->sq.counts = (uint32_t*)p[3];
+  pt->sq.fetch = pt->sq.counts + kMaxBounceSlots;
+  pt->shadow_capacity = paths;
   return NB_OK;
 }
 
@@ -465,6 +551,11 @@ static int render_samples(nb_pathtracer* pt, const nb_scene* scene, const nb_cam
     wt.n_paths = npix * S;
     wt.n_pix = npix;
     const uint32_t B = pt->globals.bounces;
+    const bool nee = (pt->sampling & NB_SAMPLE_ENV_NEE) != 0 && !pt->cache;
+    if (nee) {
+      if ((rc = ensure_shadow(pt, npix * S))) return rc;
+      NB_CUDA(cudaMemsetAsync(pt->sq.counts, 0, 2 * kMaxBounceSlots * sizeof(uint32_t), st), "cudaMemsetAsync");
+    }
     CacheWave cw{};
     if (pt->cache) {
       rc = cache_wave_begin(pt->cache, scene, wt.n_paths, &cw, st);
@@ -475,8 +566,12 @@ static int render_samples(nb_pathtracer* pt, const nb_scene* scene, const nb_cam
       e = timed_launch(pt, kKindTrace, st, [&] { return launch_trace_wave(pb, wt, true, b, pt->d_rays, pt->sms, st); });
       if (e == cudaSuccess)
         e = timed_launch(pt, kKindShade, st, [&] {
-          return pt->cache ? launch_shade_cache(pb, wt, cw, b, pt->sms, st) : launch_shade(pb, wt, b, pt->sms, st);
+          if (pt->cache) return launch_shade_cache(pb, wt, cw, b, pt->sms, st);
+          if (nee) return launch_shade_nee(pb, wt, pt->sq, b, pt->sms, st);
+          return launch_shade(pb, wt, b, pt->sms, st);
         });
+      if (e == cudaSuccess && nee)
+        e = timed_launch(pt, kKindTrace, st, [&] { return launch_trace_shadow(pb, wt, pt->sq, b, pt->sms, st); });
     }
     if (e == cudaSuccess && pt->cache) {
       rc = NB_OK;
@@ -545,6 +640,27 @@ int nb_pathtracer_kernel_times(nb_pathtracer* pt, nb_kernel_times* out, int rese
     }
     pt->timed.clear();
   }
+  return NB_OK;
+}
+
+int nb_pathtracer_set_sampling(nb_pathtracer* pt, uint32_t flags) {
+  if (!pt) return fail(NB_ERR_INVALID_ARG, "NULL argument");
+  if (flags & ~(uint32_t)NB_SAMPLE_ENV_NEE) return fail(NB_ERR_INVALID_ARG, "unknown sampling flags 0x%x", flags);
+  pt->sampling = flags;
+  return NB_OK;
+}
+
+int nb_pathtracer_get_sampling(const nb_pathtracer* pt, uint32_t* flags) {
+  if (!pt || !flags) return fail(NB_ERR_INVALID_ARG, "NULL argument");
+  *flags = pt->sampling;
+  return NB_OK;
+}
+
+int nb_env_sample(const nb_env* env, const float* u, size_t n, float* out, void* stream) {
+  if (!env || (!u && n) || (!out && n)) return fail(NB_ERR_INVALID_ARG, "NULL argument");
+  if (n > 0x7FFFFFFFull) return fail(NB_ERR_INVALID_ARG, "too many samples");
+  NB_CUDA(launch_env_sample(env->dev, u, (uint32_t)n, (float4*)out, sm_count(), (cudaStream_t)stream),
+          "env sample launch");
   return NB_OK;
 }
 

@@ -135,6 +135,12 @@ struct DevEnv {
   float r, g, b;
   const float4* texels;
   uint32_t width, height;
+  // importance-sampling distribution of an equirect map (piecewise constant over texels,
+  // weight = luminance x sin(theta)): marginal CDF over rows (height + 1), conditional CDFs
+  // per row (height x (width + 1)), density over (u, v) per texel (width x height)
+  const float* cdf_rows;
+  const float* cdf_cols;
+  const float* pdf_uv;
 };
 
 }  // namespace nbd

@@ -37,6 +37,7 @@ using nb::JobParams;
 using nb::kMaxBounceSlots;
 using nb::PathBatch;
 using nb::Segment;
+using nb::ShadowQueue;
 using nb::WaveTables;
 
 constexpr int kStackSize = 64;
@@ -431,6 +432,62 @@ __device__ V3 env_lookup(const DevEnv& env, V3 dir) {
   return V3{(t00.x * (1.0f - tx) + t10.x * tx) * (1.0f - ty) + (t01.x * (1.0f - tx) + t11.x * tx) * ty,
             (t00.y * (1.0f - tx) + t10.y * tx) * (1.0f - ty) + (t01.y * (1.0f - tx) + t11.y * tx) * ty,
             (t00.z * (1.0f - tx) + t10.z * tx) * (1.0f - ty) + (t01.z * (1.0f - tx) + t11.z * tx) * ty};
+}
+
+// ---- environment importance sampling (NB_SAMPLE_ENV_NEE; no counterpart in the reference,
+// whose README lists it as planned work) ----------------------------------------------------
+
+// largest i in [0, n - 2] with c[i] <= u, for a CDF c[0] = 0 ... c[n - 1] = 1 and u in [0, 1)
+__device__ __forceinline__ uint32_t cdf_index(const float* c, uint32_t n, float u) {
+  uint32_t lo = 0, hi = n - 1;
+  while (hi - lo > 1) {
+    const uint32_t mid = (lo + hi) >> 1;
+    if (__ldg(c + mid) <= u) lo = mid;
+    else hi = mid;
+  }
+  return lo;
+}
+
+// Direction of an environment sample for uniform (u1, u2).  Constant environment: uniform on
+// the sphere.  Equirect: texel row by the marginal CDF, column by the row's CDF, uniform
+// inside the texel cell of (u, v), mapped like env_lookup: theta = pi v, phi = 2 pi (u - 1/2),
+// d = (sin theta sin phi, cos theta, -sin theta cos phi).
+__device__ V3 env_sample_dir(const DevEnv& env, float u1, float u2) {
+  if (env.kind == kEnvConstant) {
+    const float z = 1.0f - 2.0f * u1;
+    const float r = sqrtf(fmaxf(0.0f, 1.0f - z * z));
+    float sp, cp;
+    nb_sincos(kTwoPi * u2 - kPi, &sp, &cp);
+    return V3{r * cp, r * sp, z};
+  }
+  const uint32_t W = env.width, H = env.height;
+  const uint32_t y = cdf_index(env.cdf_rows, H + 1, u1);
+  const float r0 = __ldg(env.cdf_rows + y), r1 = __ldg(env.cdf_rows + y + 1);
+  const float dv = r1 > r0 ? fminf((u1 - r0) / (r1 - r0), 0.99999994f) : 0.5f;
+  const float* row = env.cdf_cols + (size_t)y * (W + 1);
+  const uint32_t x = cdf_index(row, W + 1, u2);
+  const float c0 = __ldg(row + x), c1 = __ldg(row + x + 1);
+  const float du = c1 > c0 ? fminf((u2 - c0) / (c1 - c0), 0.99999994f) : 0.5f;
+  const float u = ((float)x + du) / (float)W, v = ((float)y + dv) / (float)H;
+  float st, ct, sp, cp;
+  nb_sincos(kPi * v, &st, &ct);
+  nb_sincos(kTwoPi * (u - 0.5f), &sp, &cp);
+  return V3{st * sp, ct, -st * cp};
+}
+
+// Solid-angle density with which env_sample_dir produces the unit direction d: 1/(4 pi) for a
+// constant environment; pdf_uv of d's texel / (2 pi^2 sin theta) for an equirect map.
+__device__ float env_pdf(const DevEnv& env, V3 d) {
+  if (env.kind == kEnvConstant) return 0.0795774715f;
+  const float u = nb_atan2(d.x, -d.z) * 0.159154943f + 0.5f;
+  const float cy = fminf(fmaxf(d.y, -1.0f), 1.0f);
+  const float v = nb_acos(cy) * 0.318309886f;
+  if (u != u || v != v) return 0.0f;
+  const int W = (int)env.width, H = (int)env.height;
+  const int x = min(max((int)(u * (float)W), 0), W - 1), y = min(max((int)(v * (float)H), 0), H - 1);
+  const float sin_t = sqrtf(fmaxf(0.0f, (1.0f - cy) * (1.0f + cy)));
+  if (!(sin_t > 0.0f)) return 0.0f;
+  return __ldg(env.pdf_uv + (size_t)y * W + x) / (19.7392088f * sin_t);  // 2 pi^2
 }
 
 // sample_vndf_iso (pathtracing.wgsl:68-98)
@@ -846,6 +903,199 @@ __global__ void __launch_bounds__(256) k_shade_cache(PathBatch pb, const WaveTab
   }
 }
 
+// f cos(theta_i) of each lobe of the reference BRDF for an arbitrary direction wi, and each
+// lobe's sampling density for wi times its selection probability (the densities the lobe
+// sampling of sample_bsdf realises).  Specular: F D G2 / (4 cos_o) with the Trowbridge-Reitz
+// D and the reference's Lambda (so that f cos / pdf_vndf is the reference's F (1 + L_V) /
+// (1 + L_L + L_V)); diffuse: (1 - metallic) color response cos_i / pi.  A perfect mirror
+// (alpha = 0) has no specular part here: only lobe sampling can find it.
+struct BsdfEval {
+  V3 spec, diff;
+  float q_spec, q_diff;
+};
+
+__device__ __forceinline__ BsdfEval eval_bsdf(const HitSurface& hs, const BsdfSample& bs, V3 wi) {
+  BsdfEval ev;
+  const V3 color = hs.color;
+  const float metallic = hs.metallic;
+  const float alpha = hs.roughness * hs.roughness;
+  const float alpha2 = alpha * alpha;
+  const V3 nn = bs.n, wo = bs.wo;
+  const float cos_o = bs.cos_o, cos_i = dot(wi, nn);
+  const V3 F0 = V3{0.04f, 0.04f, 0.04f} * (1.0f - metallic) + color * metallic;
+  const float specular_weight = luminance(F_schlick(dot(wo, nn), F0));
+  const float diffuse_weight = (1.0f - metallic) * luminance(color);
+  const float p_specular = specular_weight / (specular_weight + diffuse_weight);
+  const float p_diffuse = 1.0f - p_specular;
+  const V3 wm = normalize(wi + wo);
+  if (alpha2 > 0.0f) {
+    const float nm = dot(nn, wm);
+    const float den = nm * nm * (alpha2 - 1.0f) + 1.0f;
+    const float D = alpha2 / (kPi * den * den);
+    const float LambdaV = lambda_tr(cos_o, alpha2), LambdaL = lambda_tr(cos_i, alpha2);
+    const V3 F = F_schlick(dot(wo, wm), F0);
+    ev.spec = F * (D / ((1.0f + LambdaV + LambdaL) * 4.0f * cos_o));
+    ev.q_spec = p_specular * D / (4.0f * (1.0f + LambdaV) * cos_o);
+  } else {
+    ev.spec = V3{0.0f, 0.0f, 0.0f};
+    ev.q_spec = __int_as_float(0x7f800000);
+  }
+  const float cosThetaD = dot(wi, wm);
+  const float FD90 = 0.5f + 2.0f * alpha * pow2(cosThetaD);
+  const float response = (1.0f + (FD90 - 1.0f) * pow5(1.0f - cos_i)) * (1.0f + (FD90 - 1.0f) * pow5(1.0f - cos_o));
+  ev.diff = (1.0f - metallic) * color * (response * cos_i * (1.0f / kPi));
+  ev.q_diff = p_diffuse * cos_i * (1.0f / kPi);
+  return ev;
+}
+
+__device__ __forceinline__ bool finite3(V3 v) { return isfinite(v.x) && isfinite(v.y) && isfinite(v.z); }
+
+// Shade with environment next-event estimation (NB_SAMPLE_ENV_NEE).  The path is the
+// reference's (same samples, lobe choice, VNDF / cosine sampling, Russian roulette); in
+// addition every non-emissive vertex samples one environment direction (importance sampling
+// of the environment's radiance, Sobol dimensions the reference leaves unused: sobol_0.w and
+// sobol_1.x of the bounce) and queues a shadow ray carrying that sample's contribution.  The
+// two techniques are combined per BRDF lobe with the power heuristic: an environment sample
+// weighs lobe k by p_env^2 / (q_k^2 + p_env^2), a lobe-sampled ray that escapes to the
+// environment by q^2 / (q^2 + p_env^2), q = the lobe's density (carried in q_t.w).  Where
+// next-event estimation cannot reach a direction (below the shading normal, cos_o <= 0, a
+// mirror lobe) the carried density is +inf and the lobe sample keeps full weight, so the
+// estimator stays unbiased.  Radiance accumulates per path (+=) instead of being written once.
+__global__ void __launch_bounds__(256) k_shade_nee(PathBatch pb, const WaveTables wt, const ShadowQueue sq,
+                                                   uint32_t bounce) {
+  __shared__ Segment segs[nb::kMaxWaveSegments];
+  stage_segments(segs, wt);
+  const uint32_t n = pb.counts[bounce];
+  const bool odd = (bounce & 1) != 0;
+  const float4* __restrict__ in_o = odd ? pb.q_o[1] : pb.q_o[0];
+  const float4* __restrict__ in_d = odd ? pb.q_d[1] : pb.q_d[0];
+  const float4* __restrict__ in_t = odd ? pb.q_t[1] : pb.q_t[0];
+  float4* __restrict__ out_o = odd ? pb.q_o[0] : pb.q_o[1];
+  float4* __restrict__ out_d = odd ? pb.q_d[0] : pb.q_d[1];
+  float4* __restrict__ out_t = odd ? pb.q_t[0] : pb.q_t[1];
+  const uint32_t stride = gridDim.x * blockDim.x;
+  const float kInf = __int_as_float(0x7f800000);
+  for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
+    const uint32_t i = base + threadIdx.x;
+    bool cont = false, shadow = false;
+    float4 next_o = make_float4(0.f, 0.f, 0.f, 0.f), next_d = next_o, next_t = next_o;
+    float4 sh_o = next_o, sh_d = next_o, sh_c = next_o;
+    if (i < n) {
+      const float4 O = in_o[i], D = in_d[i], Tq = in_t[i], H = pb.hits[i];
+      const uint32_t id = __float_as_uint(O.w);
+      const Segment sg = segs[find_segment<false>(segs, wt.n_segs, id)];
+      const JobParams& jp = wt.jobs[sg.job];
+      const DevScene& s = wt.scenes[jp.scene];
+      V3 T = xyz(Tq);
+      const V3 rdir = xyz(D);
+      if (H.x == kNoHit) {
+        V3 L = T * env_lookup(jp.env, rdir);
+        const float q = Tq.w;  // density of the lobe sample that made this ray (bounce > 0)
+        if (bounce > 0 && q < kInf) {
+          const float pe = env_pdf(jp.env, normalize(rdir));
+          L = L * (q * q / (q * q + pe * pe));
+        }
+        const float4 c = pb.radiance[id];
+        pb.radiance[id] = make_float4(c.x + L.x, c.y + L.y, c.z + L.z, 0.0f);
+      } else {
+        HitSurface hs;
+        load_hit_surface(s, pb.hit_inst[i], O, H, rdir, hs);
+        if (hs.emissive) {
+          const V3 L = T * hs.color;
+          const float4 c = pb.radiance[id];
+          pb.radiance[id] = make_float4(c.x + L.x, c.y + L.y, c.z + L.z, 0.0f);
+        } else {
+          const uint32_t local = id - sg.path_begin;
+          const uint32_t pix = local % jp.npix;
+          const uint32_t sample = sg.first_sample + local / jp.npix;
+          const float4 shift = hash4f(pix % jp.width, pix / jp.width);
+          float4 s0, s1;
+          bounce_samples(pb, sample, bounce, shift, s0, s1);
+          const BsdfSample bs = sample_bsdf<true>(hs, rdir, s0, s1);
+          const bool nee_ok = bs.cos_o > 0.0f;
+          if (nee_ok) {
+            const uint32_t sb = sample * kLdsStride + 1u + bounce * kLdsPerBounce;
+            const float u1 = fract(sobol_read(pb.sobol, pb.sobol_entries, sb).w + shift.w);
+            const float u2 = fract(sobol_read(pb.sobol, pb.sobol_entries, sb + 1u).x + shift.x);
+            const V3 we = env_sample_dir(jp.env, u1, u2);
+            const float pe = env_pdf(jp.env, we);
+            if (pe > 0.0f && dot(we, bs.n) > 0.0f) {
+              const BsdfEval ev = eval_bsdf(hs, bs, we);
+              const float pe2 = pe * pe;
+              const float ws = pe2 / (ev.q_spec * ev.q_spec + pe2), wd = pe2 / (ev.q_diff * ev.q_diff + pe2);
+              const V3 C = T * env_lookup(jp.env, we) * (ev.spec * ws + ev.diff * wd) / pe;
+              if (finite3(C) && (C.x > 0.0f || C.y > 0.0f || C.z > 0.0f)) {
+                shadow = true;
+                sh_o = make_float4(hs.pos.x, hs.pos.y, hs.pos.z, O.w);
+                sh_d = make_float4(we.x, we.y, we.z, 0.0f);
+                sh_c = make_float4(C.x, C.y, C.z, 0.0f);
+              }
+            }
+          }
+          T = T * bs.weight;
+          const float p_continue = rr_continue(bounce, jp.bounces, T, jp.cf);
+          if (s0.z < p_continue && bounce < jp.bounces) {
+            T = T / p_continue;
+            cont = true;
+            const float q = (nee_ok && dot(bs.wi, bs.n) > 0.0f) ? bs.pdf : kInf;
+            next_o = make_float4(hs.pos.x, hs.pos.y, hs.pos.z, O.w);
+            next_d = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, D.w);
+            next_t = make_float4(T.x, T.y, T.z, q);
+          }
+        }
+      }
+    }
+    const uint32_t slot = warp_append(pb.counts + bounce + 1, cont);
+    if (cont) {
+      out_o[slot] = next_o;
+      out_d[slot] = next_d;
+      out_t[slot] = next_t;
+    }
+    const uint32_t ss = warp_append(sq.counts + bounce, shadow);
+    if (shadow) {
+      sq.o[ss] = sh_o;
+      sq.d[ss] = sh_d;
+      sq.c[ss] = sh_c;
+    }
+  }
+}
+
+// Shadow rays of one bounce: an any-hit query each (raytracing_sw.wgsl's triangle test and
+// BIAS, so the ray leaves its own surface like the reference's extension rays); unoccluded
+// rays add their contribution to the path.  A path has at most one shadow ray per bounce, so
+// each radiance entry has one writer per launch.
+__global__ void __launch_bounds__(128) k_trace_shadow(PathBatch pb, const WaveTables wt, const ShadowQueue sq,
+                                                      uint32_t bounce) {
+  const uint32_t n = sq.counts[bounce];
+  const int lane = threadIdx.x & 31;
+  uint32_t st = 0;
+  while (true) {
+    uint32_t base = 0;
+    if (lane == 0) base = atomicAdd(sq.fetch + bounce, 32u);
+    base = __shfl_sync(0xFFFFFFFFu, base, 0);
+    if (base >= n) break;
+    const uint32_t i = base + lane;
+    if (i < n) {
+      const float4 o = sq.o[i], d = sq.d[i];
+      Hit h;
+      st |= trace_ray<true>(wt.scenes[0], xyz(o), xyz(d), h);
+      if (h.t == kNoHit) {
+        const uint32_t id = __float_as_uint(o.w);
+        const float4 c = sq.c[i], r = pb.radiance[id];
+        pb.radiance[id] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.0f);
+      }
+    }
+  }
+  if (st) atomicOr(pb.status, st);
+}
+
+__global__ void k_env_sample(const DevEnv env, const float* __restrict__ u, uint32_t n, float4* __restrict__ out) {
+  for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const V3 d = env_sample_dir(env, u[2 * i], u[2 * i + 1]);
+    out[i] = make_float4(d.x, d.y, d.z, env_pdf(env, d));
+  }
+}
+
 // running mean in sample order: out = mix(out, L_k, 1/k) (pathtracing.wgsl:246-260).  Each job
 // has at most one segment per wave, so every pixel has one writer.
 __global__ void __launch_bounds__(256) k_accumulate(PathBatch pb, const WaveTables wt) {
@@ -924,6 +1174,28 @@ cudaError_t launch_shade_cache(const PathBatch& pb, const WaveTables& wt, const 
                                int sms, cudaStream_t st) {
   static const int g = blocks_for((const void*)nbd::k_shade_cache, 256, sms);
   nbd::k_shade_cache<<<g, 256, 0, st>>>(pb, wt, cw, bounce);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_shade_nee(const PathBatch& pb, const WaveTables& wt, const ShadowQueue& sq, uint32_t bounce,
+                             int sms, cudaStream_t st) {
+  static const int g = blocks_for((const void*)nbd::k_shade_nee, 256, sms);
+  nbd::k_shade_nee<<<g, 256, 0, st>>>(pb, wt, sq, bounce);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_trace_shadow(const PathBatch& pb, const WaveTables& wt, const ShadowQueue& sq, uint32_t bounce,
+                                int sms, cudaStream_t st) {
+  static const int g = blocks_for((const void*)nbd::k_trace_shadow, 128, sms);
+  nbd::k_trace_shadow<<<g, 128, 0, st>>>(pb, wt, sq, bounce);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_env_sample(const nbd::DevEnv& env, const float* u, uint32_t n, float4* out, int sms,
+                              cudaStream_t st) {
+  if (n == 0) return cudaSuccess;
+  const int g = (int)std::min<uint64_t>((n + 255) / 256, (uint64_t)sms * 8);
+  nbd::k_env_sample<<<g, 256, 0, st>>>(env, u, n, out);
   return cudaGetLastError();
 }
 

@@ -69,6 +69,24 @@ cudaError_t launch_raygen(const PathBatch& pb, const WaveTables& wt, int sms, cu
 cudaError_t launch_trace_wave(const PathBatch& pb, const WaveTables& wt, bool single_scene, uint32_t bounce,
                               unsigned long long* ray_total, int sms, cudaStream_t st);
 cudaError_t launch_shade(const PathBatch& pb, const WaveTables& wt, uint32_t bounce, int sms, cudaStream_t st);
+// Shadow rays of environment next-event estimation: one per path and bounce at most.
+struct ShadowQueue {
+  float4* o;          // origin, .w = path id (bits)
+  float4* d;          // direction (unit)
+  float4* c;          // radiance the path gains when the direction is unoccluded
+  uint32_t* counts;   // rays appended per bounce (kMaxBounceSlots)
+  uint32_t* fetch;    // work-fetch cursor per bounce (kMaxBounceSlots)
+};
+
+// environment next-event estimation (NB_SAMPLE_ENV_NEE): shade, then the bounce's shadow rays
+cudaError_t launch_shade_nee(const PathBatch& pb, const WaveTables& wt, const ShadowQueue& sq, uint32_t bounce,
+                             int sms, cudaStream_t st);
+cudaError_t launch_trace_shadow(const PathBatch& pb, const WaveTables& wt, const ShadowQueue& sq, uint32_t bounce,
+                                int sms, cudaStream_t st);
+// directions and densities of env importance samples for uniform pairs u (device arrays)
+cudaError_t launch_env_sample(const nbd::DevEnv& env, const float* u, uint32_t n, float4* out, int sms,
+                              cudaStream_t st);
+
 struct CacheWave;
 // radiance-cache mode shade (nb_mlp.cuh describes the wave state)
 cudaError_t launch_shade_cache(const PathBatch& pb, const WaveTables& wt, const CacheWave& cw, uint32_t bounce,

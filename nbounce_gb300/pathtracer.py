@@ -169,6 +169,13 @@ class EnvMap:
     def handle(self):
         return self._h
 
+    def sample(self, u_dev, n, out_dev, stream=None):
+        """Importance samples of this environment: u (n x 2 uniform floats) -> out (n x 4:
+        direction, solid-angle density).  Device arrays (objects with data_ptr() or addresses)."""
+        up = u_dev.data_ptr() if hasattr(u_dev, "data_ptr") else int(u_dev)
+        op = out_dev.data_ptr() if hasattr(out_dev, "data_ptr") else int(out_dev)
+        check(lib().nb_env_sample(self._h, C.c_void_p(up), int(n), C.c_void_p(op), _stream(stream)))
+
     def close(self):
         if self._h:
             lib().nb_env_destroy(self._h)
@@ -258,6 +265,16 @@ class Pathtracer:
 
     def set_batch_paths(self, paths):
         check(lib().nb_pathtracer_set_batch_paths(self._h, int(paths)))
+
+    def set_sampling(self, env_nee=False):
+        """Estimator options: env_nee adds environment next-event estimation (MIS-weighted)."""
+        check(lib().nb_pathtracer_set_sampling(self._h, L.NB_SAMPLE_ENV_NEE if env_nee else 0))
+
+    @property
+    def sampling(self):
+        f = C.c_uint32()
+        check(lib().nb_pathtracer_get_sampling(self._h, C.byref(f)))
+        return {"env_nee": bool(f.value & L.NB_SAMPLE_ENV_NEE)}
 
     def set_cache(self, cache):
         """Attach a RadianceCache (None: plain path tracing).  Keep the cache alive meanwhile."""

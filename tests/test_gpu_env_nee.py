@@ -1,0 +1,141 @@
+"""Environment next-event estimation (NB_SAMPLE_ENV_NEE): the importance-sampling tables and
+the MIS-weighted estimator.
+
+* Sampling: directions drawn for uniform pairs land in each equirect texel with probability
+  w / sum(w), w = luminance x sin(theta) (histogram against that, total variation < 1%); the
+  density reported for each direction is that texel's w / sum(w) x W x H / (2 pi^2 sin theta);
+  E[1/pdf] = 4 pi (the density integrates to one over the sphere).
+* Estimator: with NEE the image converges to the plain estimator's image (same integral,
+  another estimator): mean radiance within 1%, relMSE between the two long renders small; and
+  at equal samples its error against a long plain render is much lower where a small bright
+  source (a sun disc) dominates the noise.
+"""
+import numpy as np
+import pytest
+import torch
+
+import nbounce_gb300 as nb
+from nbounce_gb300 import scenes
+
+pytestmark = pytest.mark.gpu
+
+
+def rel_mse(a, b):
+    a = a[..., :3].astype(np.float64)
+    b = b[..., :3].astype(np.float64)
+    ok = np.all(np.isfinite(a), -1) & np.all(np.isfinite(b), -1)
+    return float(np.mean(((a - b) ** 2 / (b ** 2 + 1e-2))[ok]))
+
+
+def synthetic_env(W=64, H=32, seed=3):
+    rng = np.random.default_rng(seed)
+    tex = np.ones((H, W, 4), np.float32)
+    tex[..., :3] = np.exp(rng.normal(0.0, 1.0, (H, W, 1))) * np.array([1.0, 0.8, 0.6])
+    tex[7, 40, :3] = 500.0  # a bright texel
+    return tex
+
+
+def sample(env, n, seed=0):
+    g = torch.Generator(device="cuda").manual_seed(seed)
+    u = torch.rand(n, 2, device="cuda", generator=g) * 0.9999999
+    out = torch.zeros(n, 4, device="cuda")
+    env.sample(u, n, out)
+    torch.cuda.synchronize()
+    return out.cpu().numpy().astype(np.float64)
+
+
+def texel_of(d, W, H):
+    u = np.arctan2(d[:, 0], -d[:, 2]) / (2 * np.pi) + 0.5
+    v = np.arccos(np.clip(d[:, 1], -1, 1)) / np.pi
+    return np.clip((v * H).astype(int), 0, H - 1), np.clip((u * W).astype(int), 0, W - 1)
+
+
+def test_equirect_sampling_follows_texel_weights():
+    tex = synthetic_env()
+    H, W = tex.shape[:2]
+    env = nb.EnvMap(texels=tex)
+    n = 1 << 21
+    s = sample(env, n)
+    d, pdf = s[:, :3], s[:, 3]
+    assert np.allclose(np.linalg.norm(d, axis=1), 1.0, atol=1e-5)
+    lum = 0.2126 * tex[..., 0] + 0.7152 * tex[..., 1] + 0.0722 * tex[..., 2]
+    sin_t = np.sin(np.pi * (np.arange(H) + 0.5) / H)[:, None]
+    w = lum.astype(np.float64) * sin_t
+    P = w / w.sum()
+    y, x = texel_of(d, W, H)
+    hist = np.zeros((H, W))
+    np.add.at(hist, (y, x), 1.0)
+    tv = 0.5 * np.abs(hist / n - P).sum()
+    assert tv < 0.01, tv
+    # the reported density is the texel's
+    expect = P[y, x] * W * H / (2 * np.pi ** 2 * np.sqrt(np.maximum(0, 1 - d[:, 1] ** 2)))
+    inner = (np.abs(d[:, 1]) < 0.999)
+    assert np.median(np.abs(pdf[inner] / expect[inner] - 1)) < 1e-3
+    # directions within ~2.4e-4 rad of a pole have cos(theta) == 1 in binary32, hence density 0;
+    # the renderer skips those samples (measured 1.2e-5 of all draws)
+    pos = pdf > 0
+    assert np.mean(~pos) < 1e-4
+    assert abs(np.mean(1.0 / pdf[pos]) / (4 * np.pi) - 1) < 0.02
+
+
+def test_constant_env_sampling_is_uniform():
+    env = nb.EnvMap((0.5, 0.6, 0.8))
+    s = sample(env, 1 << 20, seed=1)
+    d, pdf = s[:, :3], s[:, 3]
+    assert np.allclose(pdf, 1 / (4 * np.pi), rtol=1e-6)
+    assert np.all(np.abs(d.mean(0)) < 5e-3)
+    assert np.allclose((d ** 2).mean(0), 1 / 3, atol=5e-3)
+
+
+def render(desc, scene, env, cam, spp, nee):
+    table = nb.sobol_burley_table(max(1024, spp), 17) if spp > 1024 else None
+    pt = nb.Pathtracer(desc.width, desc.height, nb.Globals(bounces=desc.bounces), sobol_table=table)
+    pt.set_sampling(env_nee=nee)
+    pt.render(scene, cam, env, spp)
+    img = pt.download()
+    assert pt.last_stats()[1] == 0
+    return img
+
+
+def test_nee_converges_to_plain_constant_sky():
+    """Unbiasedness under a constant sky: NEE at 4096 spp against plain at 8192 spp."""
+    desc = scenes.spheres_scene(width=64, height=64, bounces=6)
+    scene = nb.SceneBuffers.from_desc(desc)
+    env = nb.EnvMap(desc.env_color)
+    cam = nb.camera_struct(desc.world_to_clip, desc.clip_to_world)
+    ref = render(desc, scene, env, cam, 8192, False)
+    nee = render(desc, scene, env, cam, 4096, True)
+    m_ref, m_nee = np.nanmean(ref[..., :3]), np.nanmean(nee[..., :3])
+    assert abs(m_nee / m_ref - 1) < 0.01, (m_nee, m_ref)
+    assert rel_mse(nee, ref) < 2e-3, rel_mse(nee, ref)
+    # no gain is expected here: under a uniform sky, cosine lobe sampling is already close to
+    # ideal and uniform sphere samples add little (measured 0.0155 vs 0.0142 at 16 spp)
+
+
+def test_nee_sun_sky_converges_and_reduces_noise():
+    """A sky with a 2-degree sun of radiance 2000: NEE at 4096 spp converges to plain at 16384
+    spp (measured mean -0.3%, relMSE 0.0013) and at 64 spp its error is far lower (13.4x)."""
+    desc = scenes.instanced_scene(scale=1 / 64, n_instances=96, width=96, height=64, env_size=(16, 8))
+    tex = scenes.sky_envmap(0x5EED9, 512, 256, sun_diameter_deg=2.0, sun_radiance=2000.0)
+    scene = nb.SceneBuffers.from_desc(desc)
+    env = nb.EnvMap(texels=tex)
+    cam = nb.camera_struct(desc.world_to_clip, desc.clip_to_world)
+    ref = render(desc, scene, env, cam, 16384, False)
+    nee = render(desc, scene, env, cam, 4096, True)
+    m_ref, m_nee = np.nanmean(ref[..., :3]), np.nanmean(nee[..., :3])
+    print(f"sun sky: mean plain16k {m_ref:.4f} nee4k {m_nee:.4f}; relMSE(nee4k, plain16k) {rel_mse(nee, ref):.5f}")
+    assert abs(m_nee / m_ref - 1) < 0.01
+    e_plain = rel_mse(render(desc, scene, env, cam, 64, False), ref)
+    e_nee = rel_mse(render(desc, scene, env, cam, 64, True), ref)
+    print(f"sun sky, 64 spp: relMSE plain {e_plain:.4f} nee {e_nee:.4f} (gain {e_plain / e_nee:.1f}x)")
+    assert e_nee * 3 < e_plain
+
+
+def test_sampling_flag_roundtrip_and_default():
+    pt = nb.Pathtracer(8, 8)
+    assert pt.sampling == {"env_nee": False}
+    pt.set_sampling(env_nee=True)
+    assert pt.sampling == {"env_nee": True}
+    from nbounce_gb300._lib import check
+    with pytest.raises(nb.NbError):
+        check(nb.lib().nb_pathtracer_set_sampling(pt._h, 0x80))
