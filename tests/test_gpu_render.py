@@ -118,3 +118,18 @@ def test_instanced_scene_crop_matches_oracle():
     assert status == 0
     assert np.mean(np.all(img == ref, axis=-1)) >= EXACT_FRAC
     assert rel_mse(img, ref) <= REL_MSE
+
+
+@pytest.mark.parametrize("bounces", [0, 12])
+def test_bounce_counts_outside_the_default_match_oracle(bounces):
+    """bounces = 0 (primary hits only) and bounces = 12: past bounce 8 the per-bounce Sobol reads
+    run beyond the fixed row stride of 17 into the next sample's row (pathtracing.wgsl:4,
+    151-159; the reference GUI allows such counts, src/app.rs:132) - both sides reproduce it."""
+    desc = scenes.spheres_scene(width=40, height=40, spp=3, bounces=bounces)
+    orc = O.OracleScene(desc.vertices, desc.indices, desc.primitives(), dedup=True)
+    img, _, status, _ = gpu_render(desc, desc.spp)
+    ref, _, _, _ = orc.render(desc.clip_to_world, desc.width, desc.height, nb.sobol_burley_table(), 1, desc.spp,
+                              bounces=desc.bounces, env=desc.env_color)
+    assert status == 0
+    assert np.mean(np.all(img == ref, axis=-1)) >= EXACT_FRAC
+    assert rel_mse(img, ref) <= REL_MSE

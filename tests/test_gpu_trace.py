@@ -108,3 +108,31 @@ def test_empty_query_and_miss_everything(soup):
     away[:, 4:7] = [1.0, 0.0, 0.0]
     hits, inst = gpu.trace_host(away)
     assert np.all(hits[:, 0] == NO_HIT) and np.all(inst == 0xFFFFFFFF)
+
+
+def test_axis_aligned_and_surface_origin_rays_match_oracle(soup):
+    """Directions with exactly-zero components (the box test nudges 1/0 to a large finite
+    reciprocal, the triangle test uses the true direction) and rays that start on a triangle
+    (rejected by BIAS = 0.1, raytracing_sw.wgsl:4,76) against the oracle."""
+    desc, gpu, orc = soup
+    rng = np.random.default_rng(21)
+    n = 6000
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, :3] = rng.uniform(-1.2, 1.2, (n, 3))
+    axis = rng.integers(0, 3, n)
+    sign = np.where(rng.uniform(size=n) < 0.5, -1.0, 1.0)
+    rays[np.arange(n), 4 + axis] = sign
+    # a third of the rays start at a triangle's centroid, in a random direction
+    idx = desc.indices.reshape(-1, 3)
+    pos = desc.vertices["pos"]
+    k = n // 3
+    t = rng.integers(0, len(idx), k)
+    rays[:k, :3] = pos[idx[t]].mean(axis=1)
+    d = rng.normal(size=(k, 3))
+    rays[:k, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    hits, inst = gpu.trace_host(rays)
+    rf, ru, cnt = orc.trace(rays)
+    assert cnt[:, 3].max() == 0
+    ties, both = compare_hits(hits, inst, gpu.export()["indices"], rf, ru)
+    assert both > 200
+    assert np.all(hits[:, 0][hits[:, 0] != NO_HIT] >= 0.1)
