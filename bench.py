@@ -372,21 +372,25 @@ def configs_report(args):
     ref_pt = nb.Pathtracer(256, 256, nb.Globals(bounces=6), sobol_table=nb.sobol_burley_table(16384, 17))
     ref_pt.render(scene, cam, env, 16384)
     ref = ref_pt.download()
-    pt = nb.Pathtracer(256, 256, nb.Globals(bounces=6))
-    for _ in range(3):
-        pt.invalidate()
-        pt.render(scene, cam, env, 16)
-    torch.cuda.synchronize()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    a.record()
-    for _ in range(10):
-        pt.invalidate()
-        pt.render(scene, cam, env, 16)
-    b.record()
-    b.synchronize()
-    ms = a.elapsed_time(b) / 10
-    rays, _ = pt.last_stats()
-    img = pt.download()
+
+    def gpu_frames(rr_start):
+        pt = nb.Pathtracer(256, 256, nb.Globals(bounces=6))
+        pt.set_rr_start_bounce(rr_start)
+        for _ in range(3):
+            pt.invalidate()
+            pt.render(scene, cam, env, 16)
+        torch.cuda.synchronize()
+        a.record()
+        for _ in range(10):
+            pt.invalidate()
+            pt.render(scene, cam, env, 16)
+        b.record()
+        b.synchronize()
+        return a.elapsed_time(b) / 10, pt.last_stats()[0], pt.download()
+
+    ms, rays, img = gpu_frames(0)
+    ms3, rays3, img3 = gpu_frames(3)
     osc = O.OracleScene(desc.vertices, desc.indices, desc.primitives(), dedup=True)
     t = time.perf_counter()
     cimg, crays, _, _ = osc.render(desc.clip_to_world, 256, 256, nb.sobol_burley_table(), 1, 16, bounces=6,
@@ -397,6 +401,9 @@ def configs_report(args):
                 "relmse": round(rel_mse(img, ref), 5), "nonfinite_pixels": nonfinite_pixels(img)},
         "cpu": {"mrays_s": round(crays / cs / 1e6, 2), "frame_ms": round(cs * 1e3, 1), "rays": int(crays),
                 "relmse": round(rel_mse(cimg, ref), 5), "nonfinite_pixels": nonfinite_pixels(cimg)},
+        "gpu_rr_from_bounce_3": {"mrays_s": round(rays3 / ms3 / 1e3, 1), "frame_ms": round(ms3, 3),
+                                 "rays": int(rays3), "relmse": round(rel_mse(img3, ref), 5)},
+        "rr": "reference schedule (cf 4) unless stated; the variant disables roulette before bounce 3",
         "reference": "16,384-spp plain GPU render", "reference_nonfinite_pixels": nonfinite_pixels(ref)}
     # soup traversal
     desc = scenes.soup_scene(1 << 20)

@@ -255,6 +255,11 @@ int nb_pathtracer_kernel_times(nb_pathtracer* pt, nb_kernel_times* out, int rese
  * cache is attached. */
 enum { NB_SAMPLE_ENV_NEE = 1u << 0 };
 int nb_pathtracer_set_sampling(nb_pathtracer* pt, uint32_t flags);
+/* Russian roulette schedule.  0 (default): the reference's, survival min(1 - (b/B)^8, 1) x
+ * min(lum(T) cf, 1) at every bounce b (pathtracing.wgsl:225-236).  n > 0: survival 1 at
+ * bounces b < n, the reference's from b = n on - the "RR from bounce 3" of the benchmark
+ * configurations (n = 3).  The expected image is the same; only the noise and cost change. */
+int nb_pathtracer_set_rr_start_bounce(nb_pathtracer* pt, uint32_t bounce);
 int nb_pathtracer_get_sampling(const nb_pathtracer* pt, uint32_t* flags);
 /* Environment importance samples: for n uniform pairs u (device, 2n floats) writes n x
  * (direction xyz, solid-angle density) to out (device, 4n floats).  Stream-ordered. */

@@ -177,6 +177,7 @@ def lib():
         "nb_cache_get_stats": ([vp, vp, vp], i32),
         "nb_pathtracer_set_cache": ([vp, vp], i32),
         "nb_pathtracer_set_sampling": ([vp, u32], i32),
+        "nb_pathtracer_set_rr_start_bounce": ([vp, u32], i32),
         "nb_pathtracer_get_sampling": ([vp, vp], i32),
         "nb_env_sample": ([vp, vp, sz, vp, vp], i32),
     }

@@ -59,6 +59,7 @@ struct nb_pathtracer {
   uint32_t batch_paths = 1u << 27;
   nb_cache* cache = nullptr;  // radiance-cache mode when set
   uint32_t sampling = 0;      // NB_SAMPLE_* flags
+  uint32_t rr_start = 0;      // Russian roulette start bounce (0: the reference schedule)
   DeviceArena shadow;         // shadow-ray queue of environment next-event estimation
   uint32_t shadow_capacity = 0;
   ShadowQueue sq{};
@@ -536,6 +537,7 @@ static int render_samples(nb_pathtracer* pt, const nb_scene* scene, const nb_cam
   jp.npix = npix;
   jp.bounces = pt->globals.bounces;
   jp.cf = pt->globals.contribution_factor;
+  jp.rr_start = pt->rr_start;
   while (remaining > 0) {
     uint32_t S = batch_samples(pt, remaining);
     int rc = ensure_capacity(pt, npix * S);
@@ -647,6 +649,12 @@ int nb_pathtracer_set_sampling(nb_pathtracer* pt, uint32_t flags) {
   if (!pt) return fail(NB_ERR_INVALID_ARG, "NULL argument");
   if (flags & ~(uint32_t)NB_SAMPLE_ENV_NEE) return fail(NB_ERR_INVALID_ARG, "unknown sampling flags 0x%x", flags);
   pt->sampling = flags;
+  return NB_OK;
+}
+
+int nb_pathtracer_set_rr_start_bounce(nb_pathtracer* pt, uint32_t bounce) {
+  if (!pt) return fail(NB_ERR_INVALID_ARG, "NULL argument");
+  pt->rr_start = bounce;
   return NB_OK;
 }
 

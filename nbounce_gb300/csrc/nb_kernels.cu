@@ -652,10 +652,13 @@ __device__ __forceinline__ BsdfSample sample_bsdf(const HitSurface& hs, V3 rdir,
   return out;
 }
 
-// Russian roulette probability (pathtracing.wgsl:225-236)
-__device__ __forceinline__ float rr_continue(uint32_t bounce, uint32_t bounces, V3 T, float cf) {
-  float p_continue = fminf(1.0f - pow8((float)bounce / (float)bounces), 1.0f);
-  return p_continue * fminf(luminance(T) * cf, 1.0f);
+// Russian roulette probability (pathtracing.wgsl:225-236).  rr_start > 0 is the start-bounce
+// variant (BASELINE's "RR from bounce 3"): survival 1 before that bounce, the reference's
+// schedule from it on; 0 is the reference.
+__device__ __forceinline__ float rr_continue(uint32_t bounce, const JobParams& jp, V3 T) {
+  float p_continue = fminf(1.0f - pow8((float)bounce / (float)jp.bounces), 1.0f);
+  p_continue = p_continue * fminf(luminance(T) * jp.cf, 1.0f);
+  return bounce < jp.rr_start ? 1.0f : p_continue;
 }
 
 __global__ void __launch_bounds__(256) k_shade(PathBatch pb, const WaveTables wt, uint32_t bounce) {
@@ -700,7 +703,7 @@ __global__ void __launch_bounds__(256) k_shade(PathBatch pb, const WaveTables wt
           bounce_samples(pb, sample, bounce, hash4f(pix % jp.width, pix / jp.width), s0, s1);
           const BsdfSample bs = sample_bsdf<false>(hs, rdir, s0, s1);
           T = T * bs.weight;
-          const float p_continue = rr_continue(bounce, jp.bounces, T, jp.cf);
+          const float p_continue = rr_continue(bounce, jp, T);
           if (s0.z < p_continue && bounce < jp.bounces) {
             T = T / p_continue;
             cont = true;
@@ -835,7 +838,7 @@ __global__ void __launch_bounds__(256) k_shade_cache(PathBatch pb, const WaveTab
           f = cache_features(hs, bs, id);
           Tq3 = T;
           const V3 Tn = T * bs.weight;
-          const float p_continue = rr_continue(bounce, jp.bounces, Tn, jp.cf);
+          const float p_continue = rr_continue(bounce, jp, Tn);
           const bool rr_ok = s0.z < p_continue && bounce < jp.bounces;
           // an infinite c turns the spread rule off; otherwise NaN budgets (degenerate
           // geometry) end the prefix as well
@@ -1033,7 +1036,7 @@ __global__ void __launch_bounds__(256) k_shade_nee(PathBatch pb, const WaveTable
             }
           }
           T = T * bs.weight;
-          const float p_continue = rr_continue(bounce, jp.bounces, T, jp.cf);
+          const float p_continue = rr_continue(bounce, jp, T);
           if (s0.z < p_continue && bounce < jp.bounces) {
             T = T / p_continue;
             cont = true;

@@ -26,7 +26,8 @@ struct JobParams {
   uint32_t width, height, npix;
   uint32_t bounces;
   float cf;             // contribution_factor
-  uint32_t pad[2];
+  uint32_t rr_start;    // Russian roulette from this bounce on (0: the reference schedule)
+  uint32_t pad;
 };
 
 struct Segment {

@@ -193,6 +193,7 @@ struct nb_server {
       jp.npix = npix;
       jp.bounces = j->desc.bounces;
       jp.cf = j->desc.contribution_factor;
+      jp.rr_start = 0;
       t.segs[t.n_segs++] = Segment{jslot, j->next_sample, want[i], path, pix};
       path += want[i] * npix;
       pix += npix;

@@ -276,6 +276,10 @@ class Pathtracer:
         check(lib().nb_pathtracer_get_sampling(self._h, C.byref(f)))
         return {"env_nee": bool(f.value & L.NB_SAMPLE_ENV_NEE)}
 
+    def set_rr_start_bounce(self, bounce=0):
+        """Russian roulette from this bounce on (0: the reference schedule at every bounce)."""
+        check(lib().nb_pathtracer_set_rr_start_bounce(self._h, int(bounce)))
+
     def set_cache(self, cache):
         """Attach a RadianceCache (None: plain path tracing).  Keep the cache alive meanwhile."""
         self._cache = cache

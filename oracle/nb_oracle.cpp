@@ -797,6 +797,7 @@ struct RenderArgs {
   uint32_t bounces;
   float cf;
   const or_env* env;
+  uint32_t rr_start;  // Russian roulette from this bounce on (0: the reference schedule)
 };
 
 // sample_rendering_eq (pathtracing.wgsl:161-241); counts traversal queries into *rays
@@ -855,6 +856,8 @@ static V3<R> sample_rendering_eq(const RenderArgs& a, uint32_t sample, const flo
     }
     R p_continue = wmin(R(1) - pow8(R(bounce) / R(a.bounces)), R(1));
     p_continue = p_continue * wmin(luminance(T) * R(a.cf), R(1));
+    // start-bounce variant (BASELINE's "RR from bounce 3"): no roulette before rr_start
+    if (bounce < a.rr_start) p_continue = R(1);
     if (s0.z < p_continue) {
       T = T / p_continue;
     } else {
@@ -1109,8 +1112,8 @@ void or_primary_rays(const float* c2w, uint32_t W, uint32_t H, const float* sobo
 uint64_t or_render(void* h, const float* c2w, uint32_t W, uint32_t H, const float* sobol, uint64_t sobol_n,
                    uint32_t first_sample, uint32_t spp, uint32_t bounces, float cf, const or_env* env,
                    uint32_t x0, uint32_t y0, uint32_t w, uint32_t hh, float* out_rgba, float* per_sample,
-                   int precision, int threads, uint32_t* overflow, uint64_t* counters) {
-  RenderArgs a{(const Scene*)h, c2w, W, H, sobol, sobol_n, bounces, cf, env};
+                   int precision, int threads, uint32_t* overflow, uint64_t* counters, uint32_t rr_start) {
+  RenderArgs a{(const Scene*)h, c2w, W, H, sobol, sobol_n, bounces, cf, env, rr_start};
   if (precision == 64)
     return render_region<double>(a, first_sample, spp, x0, y0, w, hh, out_rgba, per_sample, threads, overflow,
                                  counters);

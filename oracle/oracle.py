@@ -57,7 +57,7 @@ def lib():
         L.or_trace.argtypes = [vp, vp, u64, i32, vp, vp, vp, i32]
         L.or_primary_rays.argtypes = [vp, u32, u32, vp, u64, u32, vp]
         L.or_render.argtypes = [vp, vp, u32, u32, vp, u64, u32, u32, u32, f32, vp, u32, u32, u32, u32,
-                                vp, vp, i32, i32, vp, vp]
+                                vp, vp, i32, i32, vp, vp, u32]
         L.or_render.restype = u64
         _lib = L
     return _lib
@@ -160,7 +160,7 @@ class OracleScene:
 
     def render(self, clip_to_world, width, height, sobol, first_sample, spp, bounces=8, contribution_factor=4.0,
                env=(0.5, 0.6, 0.8), region=None, out=None, per_sample=False, precision=32, threads=None,
-               env_texels=None):
+               env_texels=None, rr_start=0):
         """Running-mean render of samples first_sample..first_sample+spp-1 (1-based) over a pixel region.
 
         Returns (rgba (h, w, 4) float32, traversal queries, per-sample L (h, w, spp, 4) or None, overflow)."""
@@ -184,7 +184,7 @@ class OracleScene:
         self.last_counters = np.zeros(4, np.uint64)
         rays = lib().or_render(self.h, _p(c2w), width, height, _p(sob), sob.size // 4, first_sample, spp, bounces,
                                contribution_factor, C.byref(e), x0, y0, w, h, _p(out), _p(ps), precision,
-                               threads or default_threads(), C.byref(ovf), _p(self.last_counters))
+                               threads or default_threads(), C.byref(ovf), _p(self.last_counters), rr_start)
         return out, int(rays), ps, bool(ovf.value)
 
     def work_per_ray(self):

@@ -133,3 +133,25 @@ def test_bounce_counts_outside_the_default_match_oracle(bounces):
     assert status == 0
     assert np.mean(np.all(img == ref, axis=-1)) >= EXACT_FRAC
     assert rel_mse(img, ref) <= REL_MSE
+
+
+def test_rr_from_bounce_3_matches_oracle():
+    """The start-bounce Russian roulette variant (no roulette before bounce 3, the reference's
+    schedule after) against the oracle running the same variant; it changes the image's noise
+    but not what the image converges to."""
+    desc = scenes.spheres_scene(width=40, height=40, spp=3, bounces=6)
+    scene = nb.SceneBuffers.from_desc(desc)
+    env = nb.EnvMap(desc.env_color)
+    cam = nb.camera_struct(desc.world_to_clip, desc.clip_to_world)
+    pt = nb.Pathtracer(desc.width, desc.height, nb.Globals(bounces=desc.bounces))
+    pt.set_rr_start_bounce(3)
+    pt.render(scene, cam, env, desc.spp)
+    img = pt.download()
+    assert pt.last_stats()[1] == 0
+    orc = O.OracleScene(desc.vertices, desc.indices, desc.primitives(), dedup=True)
+    ref, _, _, _ = orc.render(desc.clip_to_world, desc.width, desc.height, nb.sobol_burley_table(), 1, desc.spp,
+                              bounces=desc.bounces, env=desc.env_color, rr_start=3)
+    assert np.mean(np.all(img == ref, axis=-1)) >= EXACT_FRAC
+    assert rel_mse(img, ref) <= REL_MSE
+    plain, _, _, _ = gpu_render(desc, desc.spp)
+    assert not np.array_equal(plain, img)
