@@ -313,6 +313,15 @@ int nb_trace_rays_host(const nb_scene* scene, const float* rays, size_t n, uint3
  * ------------------------------------------------------------------------------------- */
 typedef struct nb_server nb_server;
 
+/* Per-job options.  NB_JOB_ENV_NEE: environment next-event estimation (as
+ * NB_SAMPLE_ENV_NEE); such jobs share waves with the others, whose images stay the same.
+ * NB_JOB_CACHE: render with the server's radiance cache of the job's scene (created on its
+ * first such job, trained online by every cache job on that scene; nb_cache_default_config);
+ * a cache job runs in waves of its own, and its image depends on what the cache learned
+ * before, so it is not reproducible alone vs in a mix.  The two flags are exclusive; an
+ * NB_JOB_ENV_NEE job's image is bit-identical to nb_pathtracer_render with NB_SAMPLE_ENV_NEE. */
+enum { NB_JOB_ENV_NEE = 1u << 0, NB_JOB_CACHE = 1u << 1 };
+
 typedef struct nb_job_desc {
   uint32_t scene;               /* slot from nb_server_add_scene */
   uint32_t env;                 /* slot from nb_server_add_env */
@@ -321,7 +330,7 @@ typedef struct nb_job_desc {
   uint32_t spp;                 /* samples: Sobol rows 1..spp of the server's table */
   uint32_t bounces;
   float contribution_factor;
-  uint32_t flags;               /* reserved, 0 */
+  uint32_t flags;               /* NB_JOB_* options (0: the reference estimator) */
   float* host_out;              /* optional: width*height RGBA32F copied here when done */
 } nb_job_desc;
 

@@ -26,6 +26,8 @@ NB_ENV_EQUIRECT = 1
 NB_TRACE_CLOSEST = 0
 NB_TRACE_ANY = 1
 NB_SAMPLE_ENV_NEE = 1
+NB_JOB_ENV_NEE = 1
+NB_JOB_CACHE = 2
 
 VERTEX_DTYPE = np.dtype([("pos", "<f4", 3), ("u", "<f4"), ("nrm", "<f4", 3), ("v", "<f4"), ("tan", "<f4", 4)])
 NODE_DTYPE = np.dtype([("min", "<f4", 3), ("start", "<u4"), ("max", "<f4", 3), ("end", "<u4")])

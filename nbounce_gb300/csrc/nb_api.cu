@@ -554,6 +554,7 @@ static int render_samples(nb_pathtracer* pt, const nb_scene* scene, const nb_cam
     wt.n_pix = npix;
     const uint32_t B = pt->globals.bounces;
     const bool nee = (pt->sampling & NB_SAMPLE_ENV_NEE) != 0 && !pt->cache;
+    jp.flags = nee ? kJobEnvNee : 0u;
     if (nee) {
       if ((rc = ensure_shadow(pt, npix * S))) return rc;
       NB_CUDA(cudaMemsetAsync(pt->sq.counts, 0, 2 * kMaxBounceSlots * sizeof(uint32_t), st), "cudaMemsetAsync");

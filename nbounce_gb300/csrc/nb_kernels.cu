@@ -1015,7 +1015,9 @@ __global__ void __launch_bounds__(256) k_shade_nee(PathBatch pb, const WaveTable
           float4 s0, s1;
           bounce_samples(pb, sample, bounce, shift, s0, s1);
           const BsdfSample bs = sample_bsdf<true>(hs, rdir, s0, s1);
-          const bool nee_ok = bs.cos_o > 0.0f;
+          // jobs without the flag take the plain estimator's exact path (one contribution
+          // added onto zero, lobe samples at full weight)
+          const bool nee_ok = (jp.flags & nb::kJobEnvNee) && bs.cos_o > 0.0f;
           if (nee_ok) {
             const uint32_t sb = sample * kLdsStride + 1u + bounce * kLdsPerBounce;
             const float u1 = fract(sobol_read(pb.sobol, pb.sobol_entries, sb).w + shift.w);
@@ -1030,7 +1032,7 @@ __global__ void __launch_bounds__(256) k_shade_nee(PathBatch pb, const WaveTable
               if (finite3(C) && (C.x > 0.0f || C.y > 0.0f || C.z > 0.0f)) {
                 shadow = true;
                 sh_o = make_float4(hs.pos.x, hs.pos.y, hs.pos.z, O.w);
-                sh_d = make_float4(we.x, we.y, we.z, 0.0f);
+                sh_d = make_float4(we.x, we.y, we.z, D.w);
                 sh_c = make_float4(C.x, C.y, C.z, 0.0f);
               }
             }
@@ -1066,9 +1068,13 @@ __global__ void __launch_bounds__(256) k_shade_nee(PathBatch pb, const WaveTable
 // Shadow rays of one bounce: an any-hit query each (raytracing_sw.wgsl's triangle test and
 // BIAS, so the ray leaves its own surface like the reference's extension rays); unoccluded
 // rays add their contribution to the path.  A path has at most one shadow ray per bounce, so
-// each radiance entry has one writer per launch.
+// each radiance entry has one writer per launch.  .w of a shadow ray's direction is the index
+// of its scene in the wave.
 __global__ void __launch_bounds__(128) k_trace_shadow(PathBatch pb, const WaveTables wt, const ShadowQueue sq,
                                                       uint32_t bounce) {
+  __shared__ DevScene scenes[nb::kMaxWaveScenes];
+  for (uint32_t i = threadIdx.x; i < wt.n_scenes; i += blockDim.x) scenes[i] = wt.scenes[i];
+  __syncthreads();
   const uint32_t n = sq.counts[bounce];
   const int lane = threadIdx.x & 31;
   uint32_t st = 0;
@@ -1081,7 +1087,7 @@ __global__ void __launch_bounds__(128) k_trace_shadow(PathBatch pb, const WaveTa
     if (i < n) {
       const float4 o = sq.o[i], d = sq.d[i];
       Hit h;
-      st |= trace_ray<true>(wt.scenes[0], xyz(o), xyz(d), h);
+      st |= trace_ray<true>(scenes[__float_as_uint(d.w)], xyz(o), xyz(d), h);
       if (h.t == kNoHit) {
         const uint32_t id = __float_as_uint(o.w);
         const float4 c = sq.c[i], r = pb.radiance[id];

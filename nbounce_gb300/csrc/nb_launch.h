@@ -27,8 +27,9 @@ struct JobParams {
   uint32_t bounces;
   float cf;             // contribution_factor
   uint32_t rr_start;    // Russian roulette from this bounce on (0: the reference schedule)
-  uint32_t pad;
+  uint32_t flags;       // kJobEnvNee: environment next-event estimation (k_shade_nee)
 };
+constexpr uint32_t kJobEnvNee = 1u << 0;
 
 struct Segment {
   uint32_t job;           // index into WaveTables::jobs

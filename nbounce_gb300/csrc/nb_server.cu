@@ -13,6 +13,13 @@
 // Jobs that arrive while waves run join the next wave.  Every path depends only on its own
 // job, pixel and sample, and a job's samples reach its image in sample order, so a job's
 // image does not depend on what it was batched with.
+//
+// Per-job options (nb_job_desc.flags): NB_JOB_ENV_NEE jobs share the ordinary waves, which
+// then run the next-event-estimation shade kernel gated per job (the other jobs' paths are
+// unchanged).  NB_JOB_CACHE jobs run in waves of their own with the radiance cache of their
+// scene (one per scene slot, created on first use, trained by every cache wave on it); when
+// both kinds are pending the scheduler alternates between a cache wave and an ordinary one.
+// The caches' buffers are outside the HBM budget's accounting.
 
 #include <algorithm>
 #include <chrono>
@@ -26,6 +33,7 @@
 #include <thread>
 #include <vector>
 
+#include "nb_mlp.cuh"
 #include "nb_runtime.h"
 
 namespace nb {
@@ -66,6 +74,9 @@ struct nb_server {
   uint32_t* d_counts = nullptr;
   unsigned long long* d_rays = nullptr;
   uint64_t fixed_bytes = 0;  // path buffers + tables
+  ShadowQueue sq{};          // shadow rays of NB_JOB_ENV_NEE jobs
+  std::map<uint32_t, nb_cache*> caches;  // scene slot -> radiance cache of NB_JOB_CACHE jobs
+  bool last_wave_cache = false;
 
   std::vector<const nb_scene*> scenes;
   std::vector<const nb_env*> envs;
@@ -144,11 +155,11 @@ struct nb_server {
   }
 
   // plans one wave into *wt; returns false if no active job has samples left to plan
-  bool plan_locked(std::vector<Job*>* wave_jobs, uint32_t* max_bounces, bool* single_scene) {
+  bool plan_locked(std::vector<Job*>* wave_jobs, uint32_t* max_bounces, bool* single_scene, bool* any_nee) {
     WaveTables& t = *wt;
     std::vector<Job*> cand;
     for (Job* j : active)
-      if (!j->fully_planned) cand.push_back(j);
+      if (!j->fully_planned && !(j->desc.flags & NB_JOB_CACHE)) cand.push_back(j);
     if (cand.empty()) return false;
     const uint64_t share = std::max<uint64_t>(1, capacity / cand.size());
     uint64_t left = capacity;
@@ -178,6 +189,7 @@ struct nb_server {
     }
     uint32_t path = 0, pix = 0;
     *max_bounces = 0;
+    *any_nee = false;
     for (size_t i = 0; i < cand.size(); ++i) {
       if (want[i] == 0) continue;
       Job* j = cand[i];
@@ -194,6 +206,8 @@ struct nb_server {
       jp.bounces = j->desc.bounces;
       jp.cf = j->desc.contribution_factor;
       jp.rr_start = 0;
+      jp.flags = (j->desc.flags & NB_JOB_ENV_NEE) ? kJobEnvNee : 0u;
+      *any_nee = *any_nee || jp.flags != 0u;
       t.segs[t.n_segs++] = Segment{jslot, j->next_sample, want[i], path, pix};
       path += want[i] * npix;
       pix += npix;
@@ -211,15 +225,88 @@ struct nb_server {
     return t.n_segs > 0;
   }
 
-  cudaError_t launch_wave(uint32_t max_bounces, bool single_scene) {
+  // the oldest cache job with samples left: one segment of as many samples as one wave holds
+  bool plan_cache_locked(std::vector<Job*>* wave_jobs, uint32_t* max_bounces, uint32_t* scene) {
+    Job* j = nullptr;
+    for (Job* a : active)
+      if (!a->fully_planned && (a->desc.flags & NB_JOB_CACHE)) {
+        j = a;
+        break;
+      }
+    if (!j) return false;
+    WaveTables& t = *wt;
+    const uint32_t npix = j->desc.width * j->desc.height;
+    const uint32_t remaining = j->desc.spp - (j->next_sample - 1);
+    const uint32_t S = std::max(1u, std::min(remaining, capacity / npix));
+    t.n_segs = t.n_jobs = t.n_scenes = 1;
+    JobParams& jp = t.jobs[0];
+    std::memcpy(jp.c2w, j->desc.camera.clip_to_world, sizeof(jp.c2w));
+    jp.env = envs[j->desc.env]->dev;
+    jp.out = (float4*)j->d_img;
+    jp.scene = 0;
+    jp.width = j->desc.width;
+    jp.height = j->desc.height;
+    jp.npix = npix;
+    jp.bounces = j->desc.bounces;
+    jp.cf = j->desc.contribution_factor;
+    jp.rr_start = 0;
+    jp.flags = 0;
+    t.segs[0] = Segment{0u, j->next_sample, S, 0u, 0u};
+    t.scenes[0] = scenes[j->desc.scene]->dev;
+    t.n_paths = S * npix;
+    t.n_pix = npix;
+    j->next_sample += S;
+    j->fully_planned = j->next_sample > j->desc.spp;
+    j->planned_waves += 1;
+    *max_bounces = j->desc.bounces;
+    *scene = j->desc.scene;
+    wave_jobs->push_back(j);
+    return true;
+  }
+
+  bool cache_job_pending_locked() const {
+    for (Job* a : active)
+      if (!a->fully_planned && (a->desc.flags & NB_JOB_CACHE)) return true;
+    return false;
+  }
+  bool plain_job_pending_locked() const {
+    for (Job* a : active)
+      if (!a->fully_planned && !(a->desc.flags & NB_JOB_CACHE)) return true;
+    return false;
+  }
+
+  cudaError_t launch_wave(uint32_t max_bounces, bool single_scene, bool nee) {
     PathBatch p = pb;
-    cudaError_t e = launch_raygen(p, *wt, sms, stream);
+    cudaError_t e = cudaSuccess;
+    if (nee) e = cudaMemsetAsync(sq.counts, 0, 2 * kMaxBounceSlots * sizeof(uint32_t), stream);
+    if (e == cudaSuccess) e = launch_raygen(p, *wt, sms, stream);
     for (uint32_t b = 0; b <= max_bounces && e == cudaSuccess; ++b) {
       e = launch_trace_wave(p, *wt, single_scene, b, d_rays, sms, stream);
-      if (e == cudaSuccess) e = launch_shade(p, *wt, b, sms, stream);
+      if (e == cudaSuccess) e = nee ? launch_shade_nee(p, *wt, sq, b, sms, stream) : launch_shade(p, *wt, b, sms, stream);
+      if (e == cudaSuccess && nee) e = launch_trace_shadow(p, *wt, sq, b, sms, stream);
     }
     if (e == cudaSuccess) e = launch_accumulate(p, *wt, sms, stream);
     return e;
+  }
+
+  // a cache wave: the plain prefix kernels with cache-mode shading, lookups and training
+  int launch_cache_wave(uint32_t scene_slot, uint32_t max_bounces) {
+    nb_cache*& c = caches[scene_slot];
+    int rc = NB_OK;
+    if (!c && (rc = nb_cache_create(nullptr, &c))) return rc;
+    CacheWave cw{};
+    if ((rc = cache_wave_begin(c, scenes[scene_slot], wt->n_paths, &cw, stream))) return rc;
+    PathBatch p = pb;
+    cudaError_t e = launch_raygen(p, *wt, sms, stream);
+    for (uint32_t b = 0; b <= max_bounces && e == cudaSuccess; ++b) {
+      e = launch_trace_wave(p, *wt, true, b, d_rays, sms, stream);
+      if (e == cudaSuccess) e = launch_shade_cache(p, *wt, cw, b, sms, stream);
+    }
+    if (e != cudaSuccess) return cuda_fail(e, "cache wave launch");
+    if ((rc = cache_wave_infer(c, p, sms, stream)) || (rc = cache_wave_train(c, wt->n_paths, sms, stream)))
+      return rc;
+    e = launch_accumulate(p, *wt, sms, stream);
+    return e == cudaSuccess ? NB_OK : cuda_fail(e, "cache wave launch");
   }
 
   void complete_locked(Job* j) {
@@ -245,19 +332,29 @@ struct nb_server {
       bool launched = false;
       if (inflight.size() < 2) {
         std::vector<Job*> wave_jobs;
-        uint32_t max_bounces = 0;
-        bool single = true;
-        if (plan_locked(&wave_jobs, &max_bounces, &single)) {
+        uint32_t max_bounces = 0, cache_scene = 0;
+        bool single = true, nee = false;
+        const bool want_cache =
+            cache_job_pending_locked() && (!plain_job_pending_locked() || !last_wave_cache);
+        const bool planned = want_cache ? plan_cache_locked(&wave_jobs, &max_bounces, &cache_scene)
+                                        : plan_locked(&wave_jobs, &max_bounces, &single, &nee);
+        if (planned) {
           InFlight w;
           w.start = take_event();
           w.stop = take_event();
           w.jobs = std::move(wave_jobs);
           cudaEventRecord(w.start, stream);
-          cudaError_t e = launch_wave(max_bounces, single);
+          int rc = NB_OK;
+          if (want_cache) {
+            rc = launch_cache_wave(cache_scene, max_bounces);
+          } else {
+            cudaError_t e = launch_wave(max_bounces, single, nee);
+            if (e != cudaSuccess) rc = cuda_fail(e, "wave launch");
+          }
+          last_wave_cache = want_cache;
           cudaEventRecord(w.stop, stream);
-          if (e != cudaSuccess) {
-            cuda_fail(e, "wave launch");
-            fail_all(NB_ERR_CUDA);
+          if (rc != NB_OK) {
+            fail_all(rc);
             return;
           }
           ++waves;
@@ -312,9 +409,10 @@ int nb_server_create(uint64_t hbm_budget_bytes, uint32_t paths_per_wave, nb_serv
   cudaGetDevice(&s->device);
   NB_CUDA(cudaStreamCreateWithFlags(&s->stream, cudaStreamNonBlocking), "cudaStreamCreate");
   NB_CUDA(cudaStreamCreateWithFlags(&s->copy_stream, cudaStreamNonBlocking), "cudaStreamCreate");
-  // path buffers: 8 float4 queues/hits/radiance + instance ids, per path
+  // path buffers: 8 float4 queues/hits/radiance + instance ids, per path; 3 float4 of
+  // shadow rays per path for NB_JOB_ENV_NEE jobs
   const size_t n_paths = paths_per_wave;
-  const size_t path_bytes = n_paths * (8 * sizeof(float4) + sizeof(uint32_t));
+  const size_t path_bytes = n_paths * (11 * sizeof(float4) + sizeof(uint32_t)) + 2 * kMaxBounceSlots * sizeof(uint32_t);
   std::vector<float> table((size_t)kMaxSampleCount * kLdsStride * 4);
   sobol_burley_table(kMaxSampleCount, kLdsStride, 0, table.data());
   const size_t table_bytes = table.size() * sizeof(float);
@@ -332,6 +430,16 @@ int nb_server_create(uint64_t hbm_budget_bytes, uint32_t paths_per_wave, nb_serv
   }
   int st = s->buffers.alloc(n_paths * sizeof(uint32_t), &p);
   if (st) { s->buffers.release(); return st; }
+  float4* shadow[3];
+  for (int k = 0; k < 3; ++k) {
+    if ((st = s->buffers.alloc(n_paths * sizeof(float4), (void**)&shadow[k]))) { s->buffers.release(); return st; }
+  }
+  uint32_t* shadow_counts = nullptr;
+  if ((st = s->buffers.alloc(2 * kMaxBounceSlots * sizeof(uint32_t), (void**)&shadow_counts))) {
+    s->buffers.release();
+    return st;
+  }
+  s->sq = ShadowQueue{shadow[0], shadow[1], shadow[2], shadow_counts, shadow_counts + kMaxBounceSlots};
   PathBatch& b = s->pb;
   b.q_o[0] = f4[0]; b.q_o[1] = f4[1];
   b.q_d[0] = f4[2]; b.q_d[1] = f4[3];
@@ -381,6 +489,9 @@ int nb_server_submit(nb_server* s, const nb_job_desc* desc, uint64_t* job_id) {
   if (desc->spp > kMaxSampleCount) return fail(NB_ERR_INVALID_ARG, "spp above the Sobol table (%u rows)", kMaxSampleCount);
   if (desc->bounces + 2 > kMaxBounceSlots) return fail(NB_ERR_INVALID_ARG, "bounces must be <= %u", kMaxBounceSlots - 2);
   if (npix > s->capacity) return fail(NB_ERR_INVALID_ARG, "image larger than the paths of one wave");
+  if (desc->flags & ~(uint32_t)(NB_JOB_ENV_NEE | NB_JOB_CACHE)) return fail(NB_ERR_INVALID_ARG, "unknown job flags 0x%x", desc->flags);
+  if ((desc->flags & NB_JOB_ENV_NEE) && (desc->flags & NB_JOB_CACHE))
+    return fail(NB_ERR_INVALID_ARG, "NB_JOB_ENV_NEE and NB_JOB_CACHE are exclusive");
   std::lock_guard<std::mutex> lk(s->mu);
   if (desc->scene >= s->scenes.size() || desc->env >= s->envs.size())
     return fail(NB_ERR_INVALID_ARG, "unknown scene or environment slot");
@@ -485,6 +596,7 @@ void nb_server_destroy(nb_server* s) {
   for (auto& kv : s->jobs)
     if (kv.second->d_img) cudaFree(kv.second->d_img);
   for (cudaEvent_t e : s->event_pool) cudaEventDestroy(e);
+  for (auto& kv : s->caches) nb_cache_destroy(kv.second);
   s->buffers.release();
   cudaStreamDestroy(s->stream);
   cudaStreamDestroy(s->copy_stream);

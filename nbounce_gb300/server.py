@@ -37,13 +37,17 @@ class RenderServer:
         return slot.value
 
     def submit(self, scene, env, world_to_clip, clip_to_world, width, height, spp, bounces=8,
-               contribution_factor=4.0, out=None):
-        """Queues a job; `out` (h, w, 4) float32 receives the image when it finishes."""
+               contribution_factor=4.0, out=None, flags=0):
+        """Queues a job; `out` (h, w, 4) float32 receives the image when it finishes.
+
+        `flags`: NB_JOB_ENV_NEE (environment next-event estimation) or NB_JOB_CACHE (the
+        server's radiance cache of the scene), 0 for the reference estimator."""
         d = L.NbJobDesc()
         d.scene, d.env = scene, env
         d.camera = camera_struct(world_to_clip, clip_to_world)
         d.width, d.height, d.spp, d.bounces = width, height, spp, bounces
         d.contribution_factor = contribution_factor
+        d.flags = flags
         d.host_out = None if out is None else out.ctypes.data
         jid = C.c_uint64()
         check(lib().nb_server_submit(self._h, C.byref(d), C.byref(jid)))

@@ -8,16 +8,17 @@ import numpy as np
 import pytest
 
 import nbounce_gb300 as nb
+from nbounce_gb300 import _lib as L
 from nbounce_gb300 import scenes
 from nbounce_gb300.server import RenderServer
 
 pytestmark = pytest.mark.gpu
 
-PATH_BYTES = 8 * 16 + 4  # per path of the server's buffers
+PATH_BYTES = 11 * 16 + 4  # per path of the server's buffers (queues, hits, radiance, shadow rays)
 
 
 def fixed_bytes(paths):
-    return paths * PATH_BYTES + 1024 * 17 * 16 + 2 * 64 * 4 + 16 + 8
+    return paths * PATH_BYTES + 2 * 64 * 4 + 1024 * 17 * 16 + 2 * 64 * 4 + 16 + 8
 
 
 @pytest.fixture(scope="module")
@@ -32,10 +33,10 @@ def world():
     return dict(descs=(sph, ins), scenes=(s0, s1), envs=(e0, e1))
 
 
-def alone(world, k, w, h, spp, bounces):
-    desc = world["descs"][k]
+def alone(world, k, w, h, spp, bounces, env_nee=False):
     w2c, c2w = scenes.camera_matrices(*CAMS[k], w, h)
     pt = nb.Pathtracer(w, h, nb.Globals(bounces=bounces))
+    pt.set_sampling(env_nee=env_nee)
     pt.render(world["scenes"][k], nb.camera_struct(w2c, c2w), world["envs"][k], spp)
     return pt.download()
 
@@ -107,4 +108,66 @@ def test_invalid_jobs_are_rejected(world):
     assert info["done"] == 1
     img = srv.fetch(job, 32, 32)
     assert np.array_equal(img, alone(world, 0, 32, 32, 2, 8))
+    srv.close()
+
+
+def test_nee_jobs_share_waves_and_equal_jobs_rendered_alone(world):
+    """NB_JOB_ENV_NEE jobs ride in the same waves as reference-estimator jobs; every image
+    equals its job rendered alone with the matching sampling mode."""
+    paths = 1 << 14
+    srv = RenderServer(hbm_budget_bytes=1 << 30, paths_per_wave=paths)
+    slots = [srv.add_scene(s) for s in world["scenes"]]
+    env_slots = [srv.add_env(e) for e in world["envs"]]
+    flags = [L.NB_JOB_ENV_NEE if i % 2 else 0 for i in range(len(JOBS))]
+    outs = [np.full((h, w, 4), np.nan, np.float32) for (_, w, h, _, _) in JOBS]
+    ids = []
+    for (k, w, h, spp, b), out, f in zip(JOBS, outs, flags):
+        w2c, c2w = scenes.camera_matrices(*CAMS[k], w, h)
+        ids.append(srv.submit(slots[k], env_slots[k], w2c, c2w, w, h, spp, b, out=out, flags=f))
+    infos = [srv.wait(j, timeout_ms=120000) for j in ids]
+    assert all(i["done"] == 1 and i["status"] == 0 for i in infos)
+    assert srv.stats()["waves"] > 1
+    for (k, w, h, spp, b), out, f in zip(JOBS, outs, flags):
+        ref = alone(world, k, w, h, spp, b, env_nee=bool(f))
+        assert np.array_equal(out, ref), (k, w, h, spp, b, f)
+    # the NEE estimator changes the image (same job, other estimator)
+    k, w, h, spp, b = JOBS[1]
+    assert not np.array_equal(outs[1], alone(world, k, w, h, spp, b))
+    srv.close()
+
+
+def test_cache_jobs_run_beside_plain_jobs(world):
+    """NB_JOB_CACHE jobs run in cache waves alternated with ordinary waves: they finish with
+    finite images, and the ordinary jobs' images stay equal to rendering them alone."""
+    paths = 1 << 14
+    srv = RenderServer(hbm_budget_bytes=1 << 30, paths_per_wave=paths)
+    slots = [srv.add_scene(s) for s in world["scenes"]]
+    env_slots = [srv.add_env(e) for e in world["envs"]]
+    flags = [L.NB_JOB_CACHE if i in (1, 2) else 0 for i in range(len(JOBS))]
+    outs = [np.full((h, w, 4), np.nan, np.float32) for (_, w, h, _, _) in JOBS]
+    ids = []
+    for (k, w, h, spp, b), out, f in zip(JOBS, outs, flags):
+        w2c, c2w = scenes.camera_matrices(*CAMS[k], w, h)
+        ids.append(srv.submit(slots[k], env_slots[k], w2c, c2w, w, h, spp, b, out=out, flags=f))
+    infos = [srv.wait(j, timeout_ms=120000) for j in ids]
+    assert all(i["done"] == 1 and i["status"] == 0 for i in infos)
+    for (k, w, h, spp, b), out, f in zip(JOBS, outs, flags):
+        if f:
+            assert np.isfinite(out).all() and (out[..., :3] >= 0).all() and (out[..., 3] == 1.0).all()
+            assert out[..., :3].mean() > 0
+        else:
+            assert np.array_equal(out, alone(world, k, w, h, spp, b)), (k, w, h, spp, b)
+    srv.close()
+
+
+def test_job_flags_are_validated(world):
+    paths = 1 << 12
+    srv = RenderServer(hbm_budget_bytes=1 << 30, paths_per_wave=paths)
+    slot = srv.add_scene(world["scenes"][0])
+    env = srv.add_env(world["envs"][0])
+    w2c, c2w = scenes.camera_matrices(*CAMS[0], 32, 32)
+    for bad in (4, 1 << 31, L.NB_JOB_ENV_NEE | L.NB_JOB_CACHE):
+        with pytest.raises(nb.NbError) as e:
+            srv.submit(slot, env, w2c, c2w, 32, 32, 1, flags=bad)
+        assert e.value.status == 1
     srv.close()
