@@ -235,10 +235,23 @@ def serving_report(args):
     server.run_load(srv, slots, env, cams, server.make_trace(8, 1000.0, len(descs), seed=1))  # warm-up
     out = {"scenes_unique_triangles": [int(d.n_triangles_unique) for d in descs], "budget_gb": 120,
            "paths_per_wave": 1 << 25, "loads": []}
+    def rounded(r):
+        return {k: (rounded(v) if isinstance(v, dict) else round(v, 3) if isinstance(v, float) else v)
+                for k, v in r.items()}
+
     for rate, n_jobs in args.serving_loads:
         r = server.run_load(srv, slots, env, cams, server.make_trace(n_jobs, rate, len(descs), seed=int(rate)))
         r["rate_jobs_per_s"] = rate
-        out["loads"].append({k: (round(v, 3) if isinstance(v, float) else v) for k, v in r.items()})
+        out["loads"].append(rounded(r))
+    # per-job estimator options: the middle load again, each job drawn from {reference,
+    # environment NEE, radiance cache}; the caches of the scenes are created by a warm-up mix
+    options = (0, server.L.NB_JOB_ENV_NEE, server.L.NB_JOB_CACHE)
+    server.run_load(srv, slots, env, cams, server.make_trace(16, 1000.0, len(descs), seed=2, options=options))
+    rate, n_jobs = args.serving_loads[len(args.serving_loads) // 2]
+    r = server.run_load(srv, slots, env, cams,
+                        server.make_trace(n_jobs, rate, len(descs), seed=int(rate), options=options))
+    r["rate_jobs_per_s"] = rate
+    out["mixed_options"] = rounded(r)
     srv.close()
     return out
 

@@ -317,8 +317,9 @@ typedef struct nb_server nb_server;
  * NB_SAMPLE_ENV_NEE); such jobs share waves with the others, whose images stay the same.
  * NB_JOB_CACHE: render with the server's radiance cache of the job's scene (created on its
  * first such job, trained online by every cache job on that scene; nb_cache_default_config);
- * a cache job runs in waves of its own, and its image depends on what the cache learned
- * before, so it is not reproducible alone vs in a mix.  The two flags are exclusive; an
+ * cache jobs run in cache waves of their own (one scene per wave), and a job's image depends
+ * on what the cache learned before, so it is not reproducible alone vs in a mix.  The two
+ * flags are exclusive; an
  * NB_JOB_ENV_NEE job's image is bit-identical to nb_pathtracer_render with NB_SAMPLE_ENV_NEE. */
 enum { NB_JOB_ENV_NEE = 1u << 0, NB_JOB_CACHE = 1u << 1 };
 

@@ -17,7 +17,8 @@
 // Per-job options (nb_job_desc.flags): NB_JOB_ENV_NEE jobs share the ordinary waves, which
 // then run the next-event-estimation shade kernel gated per job (the other jobs' paths are
 // unchanged).  NB_JOB_CACHE jobs run in waves of their own with the radiance cache of their
-// scene (one per scene slot, created on first use, trained by every cache wave on it); when
+// scene (one per scene slot, created on first use, trained by every cache wave on it); a cache
+// wave packs the pending cache jobs of one scene like an ordinary wave packs the others.  When
 // both kinds are pending the scheduler alternates between a cache wave and an ordinary one.
 // The caches' buffers are outside the HBM budget's accounting.
 
@@ -155,11 +156,14 @@ struct nb_server {
   }
 
   // plans one wave into *wt; returns false if no active job has samples left to plan
-  bool plan_locked(std::vector<Job*>* wave_jobs, uint32_t* max_bounces, bool* single_scene, bool* any_nee) {
+  // packs the unplanned active jobs that `pick` accepts into the next wave
+  template <class Pick>
+  bool plan_locked(std::vector<Job*>* wave_jobs, uint32_t* max_bounces, bool* single_scene, bool* any_nee,
+                   Pick pick) {
     WaveTables& t = *wt;
     std::vector<Job*> cand;
     for (Job* j : active)
-      if (!j->fully_planned && !(j->desc.flags & NB_JOB_CACHE)) cand.push_back(j);
+      if (!j->fully_planned && pick(j)) cand.push_back(j);
     if (cand.empty()) return false;
     const uint64_t share = std::max<uint64_t>(1, capacity / cand.size());
     uint64_t left = capacity;
@@ -225,43 +229,20 @@ struct nb_server {
     return t.n_segs > 0;
   }
 
-  // the oldest cache job with samples left: one segment of as many samples as one wave holds
+  // a cache wave: the cache jobs on the scene of the oldest cache job with samples left
   bool plan_cache_locked(std::vector<Job*>* wave_jobs, uint32_t* max_bounces, uint32_t* scene) {
-    Job* j = nullptr;
-    for (Job* a : active)
+    const Job* first = nullptr;
+    for (const Job* a : active)
       if (!a->fully_planned && (a->desc.flags & NB_JOB_CACHE)) {
-        j = a;
+        first = a;
         break;
       }
-    if (!j) return false;
-    WaveTables& t = *wt;
-    const uint32_t npix = j->desc.width * j->desc.height;
-    const uint32_t remaining = j->desc.spp - (j->next_sample - 1);
-    const uint32_t S = std::max(1u, std::min(remaining, capacity / npix));
-    t.n_segs = t.n_jobs = t.n_scenes = 1;
-    JobParams& jp = t.jobs[0];
-    std::memcpy(jp.c2w, j->desc.camera.clip_to_world, sizeof(jp.c2w));
-    jp.env = envs[j->desc.env]->dev;
-    jp.out = (float4*)j->d_img;
-    jp.scene = 0;
-    jp.width = j->desc.width;
-    jp.height = j->desc.height;
-    jp.npix = npix;
-    jp.bounces = j->desc.bounces;
-    jp.cf = j->desc.contribution_factor;
-    jp.rr_start = 0;
-    jp.flags = 0;
-    t.segs[0] = Segment{0u, j->next_sample, S, 0u, 0u};
-    t.scenes[0] = scenes[j->desc.scene]->dev;
-    t.n_paths = S * npix;
-    t.n_pix = npix;
-    j->next_sample += S;
-    j->fully_planned = j->next_sample > j->desc.spp;
-    j->planned_waves += 1;
-    *max_bounces = j->desc.bounces;
-    *scene = j->desc.scene;
-    wave_jobs->push_back(j);
-    return true;
+    if (!first) return false;
+    const uint32_t sc = first->desc.scene;
+    bool single = true, nee = false;
+    *scene = sc;
+    return plan_locked(wave_jobs, max_bounces, &single, &nee,
+                       [sc](const Job* j) { return (j->desc.flags & NB_JOB_CACHE) && j->desc.scene == sc; });
   }
 
   bool cache_job_pending_locked() const {
@@ -337,7 +318,8 @@ struct nb_server {
         const bool want_cache =
             cache_job_pending_locked() && (!plain_job_pending_locked() || !last_wave_cache);
         const bool planned = want_cache ? plan_cache_locked(&wave_jobs, &max_bounces, &cache_scene)
-                                        : plan_locked(&wave_jobs, &max_bounces, &single, &nee);
+                                        : plan_locked(&wave_jobs, &max_bounces, &single, &nee,
+                                                      [](const Job* j) { return !(j->desc.flags & NB_JOB_CACHE); });
         if (planned) {
           InFlight w;
           w.start = take_event();

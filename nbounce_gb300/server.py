@@ -89,15 +89,25 @@ RESOLUTIONS = ((256, 256), (512, 512), (1024, 768), (1920, 1080))
 SPPS = (1, 4, 16, 64)
 
 
-def make_trace(n_jobs, rate_per_s, n_scenes, seed=0x5EED4, resolutions=RESOLUTIONS, spps=SPPS):
-    """Seeded Poisson arrivals: (arrival_s, scene, (w, h), spp) per job."""
+def make_trace(n_jobs, rate_per_s, n_scenes, seed=0x5EED4, resolutions=RESOLUTIONS, spps=SPPS, options=None):
+    """Seeded Poisson arrivals: (arrival_s, scene, (w, h), spp, flags) per job.
+
+    `options`: job flags drawn uniformly per job (from a second seeded stream, so that the
+    arrivals, scenes, sizes and sample counts equal those of the same trace without them);
+    None: every job uses the reference estimator (flags 0)."""
     rng = np.random.default_rng(seed)
+    opt_rng = np.random.default_rng(seed ^ 0x0F7105)
     t = np.cumsum(rng.exponential(1.0 / rate_per_s, n_jobs))
     out = []
     for k in range(n_jobs):
         w, h = resolutions[rng.integers(len(resolutions))]
-        out.append((float(t[k]), int(rng.integers(n_scenes)), (int(w), int(h)), int(spps[rng.integers(len(spps))])))
+        flags = 0 if options is None else int(options[opt_rng.integers(len(options))])
+        out.append((float(t[k]), int(rng.integers(n_scenes)), (int(w), int(h)), int(spps[rng.integers(len(spps))]),
+                    flags))
     return out
+
+
+OPTION_NAMES = {0: "reference", L.NB_JOB_ENV_NEE: "env_nee", L.NB_JOB_CACHE: "cache"}
 
 
 def run_load(server, scene_slots, env_slot, cameras, trace, bounces=8):
@@ -106,13 +116,13 @@ def run_load(server, scene_slots, env_slot, cameras, trace, bounces=8):
     outs = []
     t0 = time.perf_counter()
     stats0 = server.stats()
-    for arrival, scene, (w, h), spp in trace:
+    for arrival, scene, (w, h), spp, flags in trace:
         delay = arrival - (time.perf_counter() - t0)
         if delay > 0:
             time.sleep(delay)
         out = np.empty((h, w, 4), np.float32)
         w2c, c2w = cameras[scene](w, h)
-        jobs.append(server.submit(scene_slots[scene], env_slot, w2c, c2w, w, h, spp, bounces, out=out))
+        jobs.append(server.submit(scene_slots[scene], env_slot, w2c, c2w, w, h, spp, bounces, out=out, flags=flags))
         outs.append(out)
     infos = [server.wait(j) for j in jobs]
     wall = time.perf_counter() - t0
@@ -123,7 +133,14 @@ def run_load(server, scene_slots, env_slot, cameras, trace, bounces=8):
     queue = np.array([i["admit_ms"] - i["submit_ms"] for i in infos])
     rays = stats1["rays"] - stats0["rays"]
     busy = stats1["gpu_busy_ms"] - stats0["gpu_busy_ms"]
-    return {"jobs": len(jobs), "failed": int(sum(i["status"] != 0 for i in infos)),
+    flags = np.array([job[4] for job in trace])
+    by_option = {}
+    for f in sorted(set(flags.tolist())):
+        sel = lat[flags == f]
+        by_option[OPTION_NAMES.get(f, str(f))] = {"jobs": int(sel.size), "p50_ms": float(np.percentile(sel, 50)),
+                                                  "p99_ms": float(np.percentile(sel, 99))}
+    extra = {"by_option": by_option} if len(by_option) > 1 else {}
+    return {**extra, "jobs": len(jobs), "failed": int(sum(i["status"] != 0 for i in infos)),
             "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
             "mean_ms": float(lat.mean()), "p99_queue_ms": float(np.percentile(queue, 99)),
             "wall_s": wall, "rays": int(rays), "mrays_per_s_wall": rays / wall / 1e6,

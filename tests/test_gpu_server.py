@@ -137,13 +137,14 @@ def test_nee_jobs_share_waves_and_equal_jobs_rendered_alone(world):
 
 
 def test_cache_jobs_run_beside_plain_jobs(world):
-    """NB_JOB_CACHE jobs run in cache waves alternated with ordinary waves: they finish with
-    finite images, and the ordinary jobs' images stay equal to rendering them alone."""
+    """NB_JOB_CACHE jobs run in cache waves (one scene each) alternated with ordinary waves:
+    they finish with finite images, and the ordinary jobs' images stay equal to rendering them
+    alone."""
     paths = 1 << 14
     srv = RenderServer(hbm_budget_bytes=1 << 30, paths_per_wave=paths)
     slots = [srv.add_scene(s) for s in world["scenes"]]
     env_slots = [srv.add_env(e) for e in world["envs"]]
-    flags = [L.NB_JOB_CACHE if i in (1, 2) else 0 for i in range(len(JOBS))]
+    flags = [L.NB_JOB_CACHE if i in (1, 2, 3) else 0 for i in range(len(JOBS))]  # 1 and 3 share a scene
     outs = [np.full((h, w, 4), np.nan, np.float32) for (_, w, h, _, _) in JOBS]
     ids = []
     for (k, w, h, spp, b), out, f in zip(JOBS, outs, flags):
