@@ -120,6 +120,23 @@ def test_instanced_scene_crop_matches_oracle():
     assert rel_mse(img, ref) <= REL_MSE
 
 
+@pytest.mark.parametrize("size", [(37, 23), (5, 13), (64, 3), (8, 8)])
+def test_image_sizes_off_the_8x8_tile_grid_match_oracle(size):
+    """Rays are queued in 8x8 tiles with the columns and rows outside the last whole tile
+    queued separately; every pixel of sizes off that grid (and narrower or lower than one
+    tile) gets exactly its own samples."""
+    w, h = size
+    desc = scenes.spheres_scene(width=w, height=h, spp=3, bounces=4)
+    orc = O.OracleScene(desc.vertices, desc.indices, desc.primitives(), dedup=True)
+    img, _, status, _ = gpu_render(desc, desc.spp)
+    ref, _, _, _ = orc.render(desc.clip_to_world, desc.width, desc.height, nb.sobol_burley_table(), 1, desc.spp,
+                              bounces=desc.bounces, env=desc.env_color)
+    assert status == 0
+    assert (img[..., 3] == 1.0).all()
+    assert np.mean(np.all(img == ref, axis=-1)) >= EXACT_FRAC
+    assert rel_mse(img, ref) <= REL_MSE
+
+
 @pytest.mark.parametrize("bounces", [0, 12])
 def test_bounce_counts_outside_the_default_match_oracle(bounces):
     """bounces = 0 (primary hits only) and bounces = 12: past bounce 8 the per-bounce Sobol reads
