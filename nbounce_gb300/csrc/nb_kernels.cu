@@ -552,18 +552,29 @@ __device__ __forceinline__ float lambda_tr(float ndotv, float alpha2) {  // path
   return (-1.0f + sqrtf(1.0f + alpha2 * tan2)) / 2.0f;
 }
 
-// Appends the surviving rays of one 256-thread block to the next bounce's queue grouped by
+// Appends the surviving rays of one block to the next bounce's queue grouped by
 // the octant of their direction (a counting sort over the block: one atomic per block).  The
 // block's input rays are neighbours in the image (tiled queue order), so each run of ~32
 // same-octant rays that a trace warp takes together starts from one small patch of the image
 // and points the same way; measured 12% faster secondary traversal than the input order.
 // The queue order changes no result: rays carry their path id.  Call from every thread of the
-// block (block-uniform control flow), alternating between two 64-word halves of sh from one
-// call to the next (the second barrier of a call then also protects the other half).
-constexpr int kShadeThreads = 256;
-constexpr int kShadeWarps = kShadeThreads / 32;
-static_assert(kShadeWarps * 8 == 64, "the offset scan gives each lane of one warp two (octant, warp) counts");
+// block (block-uniform control flow), alternating between two kSlots-word halves of sh from
+// one call to the next (the second barrier of a call then also protects the other half).
+template <int kThreads>
+struct AppendShape {
+  static constexpr int kWarps = kThreads / 32;
+  static constexpr int kSlots = kWarps * 8;      // (warp, octant) counts of one call
+  static constexpr int kPerLane = kSlots / 32;   // counts each lane of the scanning warp owns
+  static_assert(kThreads % 32 == 0 && kSlots % 32 == 0, "whole warps of 32 threads, 8 octants");
+};
+// k_shade: 512 threads capped at 64 registers (2 blocks per SM) measured 1.3% faster than 256
+// threads at 68 registers (3 blocks); the NEE and cache shade kernels (78 registers) stay at
+// 256 threads, where that cap would spill
+constexpr int kShadeThreads = 512;
+constexpr int kShadeExtThreads = 256;
+template <int kThreads>
 __device__ __forceinline__ uint32_t block_append_octant(uint32_t* counter, bool active, float4 dir, uint32_t* sh) {
+  using A = AppendShape<kThreads>;
   const uint32_t oct = ((dir.x < 0.0f) ? 4u : 0u) | ((dir.y < 0.0f) ? 2u : 0u) | ((dir.z < 0.0f) ? 1u : 0u);
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   const uint32_t below = (1u << lane) - 1u;
@@ -577,10 +588,15 @@ __device__ __forceinline__ uint32_t block_append_octant(uint32_t* counter, bool 
   __syncthreads();
   if (warp == 0) {
     // exclusive offsets in (octant, warp) order, i.e. runs of one octant; lane l owns the
-    // entries e = 2l and 2l + 1, stored at sh[(e % 8) * 8 + e / 8]
-    const int a = ((2 * lane) & 7) * 8 + (2 * lane) / 8, b = ((2 * lane + 1) & 7) * 8 + (2 * lane + 1) / 8;
-    const uint32_t ca = sh[a], cb = sh[b];
-    uint32_t incl = ca + cb;
+    // entries e = l * kPerLane + j, stored at sh[(e % kWarps) * 8 + e / kWarps]
+    uint32_t c[A::kPerLane], own = 0;
+#pragma unroll
+    for (int j = 0; j < A::kPerLane; ++j) {
+      const int e = lane * A::kPerLane + j;
+      c[j] = sh[(e % A::kWarps) * 8 + e / A::kWarps];
+      own += c[j];
+    }
+    uint32_t incl = own;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
       const uint32_t t = __shfl_up_sync(0xFFFFFFFFu, incl, d);
@@ -589,10 +605,13 @@ __device__ __forceinline__ uint32_t block_append_octant(uint32_t* counter, bool 
     const uint32_t total = __shfl_sync(0xFFFFFFFFu, incl, 31);
     uint32_t base = 0;
     if (lane == 0 && total) base = atomicAdd(counter, total);
-    base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    const uint32_t excl = incl - ca - cb;
-    sh[a] = base + excl;
-    sh[b] = base + excl + ca;
+    base = __shfl_sync(0xFFFFFFFFu, base, 0) + incl - own;
+#pragma unroll
+    for (int j = 0; j < A::kPerLane; ++j) {
+      const int e = lane * A::kPerLane + j;
+      sh[(e % A::kWarps) * 8 + e / A::kWarps] = base;
+      base += c[j];
+    }
   }
   __syncthreads();
   return sh[warp * 8 + oct] + rank;
@@ -736,9 +755,9 @@ __device__ __forceinline__ float rr_continue(uint32_t bounce, const JobParams& j
   return bounce < jp.rr_start ? 1.0f : p_continue;
 }
 
-__global__ void __launch_bounds__(kShadeThreads) k_shade(PathBatch pb, const WaveTables wt, uint32_t bounce) {
+__global__ void __launch_bounds__(kShadeThreads, 2) k_shade(PathBatch pb, const WaveTables wt, uint32_t bounce) {
   __shared__ Segment segs[nb::kMaxWaveSegments];
-  __shared__ uint32_t append_sh[2 * kShadeWarps * 8];
+  __shared__ uint32_t append_sh[2 * AppendShape<kShadeThreads>::kSlots];
   stage_segments(segs, wt);
   const uint32_t n = pb.counts[bounce];
   const bool odd = (bounce & 1) != 0;
@@ -790,7 +809,8 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade(PathBatch pb, const Wav
         }
       }
     }
-    const uint32_t slot = block_append_octant(pb.counts + bounce + 1, cont, next_d, append_sh + ((base / stride) & 1u) * 64);
+    const uint32_t slot = block_append_octant<kShadeThreads>(
+        pb.counts + bounce + 1, cont, next_d, append_sh + ((base / stride) & 1u) * AppendShape<kShadeThreads>::kSlots);
     if (cont) {
       out_o[slot] = next_o;
       out_d[slot] = next_d;
@@ -833,11 +853,11 @@ __device__ __forceinline__ nb::CacheFeatures cache_features(const HitSurface& hs
 //    throughput is multiplied by), continues past its query vertex for `extra` vertices and
 //    ends in a tail query that closes its radiance chain with the cache (self-training),
 //    unless a miss, an emitter or Russian roulette ends it first.
-__global__ void __launch_bounds__(kShadeThreads) k_shade_cache(PathBatch pb, const WaveTables wt, const nb::CacheWave cw,
+__global__ void __launch_bounds__(kShadeExtThreads) k_shade_cache(PathBatch pb, const WaveTables wt, const nb::CacheWave cw,
                                                      uint32_t bounce) {
   using nb::CacheQuery;
   __shared__ Segment segs[nb::kMaxWaveSegments];
-  __shared__ uint32_t append_sh[2 * kShadeWarps * 8];
+  __shared__ uint32_t append_sh[2 * AppendShape<kShadeExtThreads>::kSlots];
   stage_segments(segs, wt);
   const uint32_t n = pb.counts[bounce];
   const bool odd = (bounce & 1) != 0;
@@ -958,7 +978,8 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade_cache(PathBatch pb, con
         }
       }
     }
-    const uint32_t at = block_append_octant(pb.counts + bounce + 1, cont, next_d, append_sh + ((base / stride) & 1u) * 64);
+    const uint32_t at = block_append_octant<kShadeExtThreads>(
+        pb.counts + bounce + 1, cont, next_d, append_sh + ((base / stride) & 1u) * AppendShape<kShadeExtThreads>::kSlots);
     if (cont) {
       out_o[at] = next_o;
       out_d[at] = next_d;
@@ -1041,10 +1062,10 @@ __device__ __forceinline__ bool finite3(V3 v) { return isfinite(v.x) && isfinite
 // next-event estimation cannot reach a direction (below the shading normal, cos_o <= 0, a
 // mirror lobe) the carried density is +inf and the lobe sample keeps full weight, so the
 // estimator stays unbiased.  Radiance accumulates per path (+=) instead of being written once.
-__global__ void __launch_bounds__(kShadeThreads) k_shade_nee(PathBatch pb, const WaveTables wt, const ShadowQueue sq,
+__global__ void __launch_bounds__(kShadeExtThreads) k_shade_nee(PathBatch pb, const WaveTables wt, const ShadowQueue sq,
                                                    uint32_t bounce) {
   __shared__ Segment segs[nb::kMaxWaveSegments];
-  __shared__ uint32_t append_sh[2 * kShadeWarps * 8];
+  __shared__ uint32_t append_sh[2 * AppendShape<kShadeExtThreads>::kSlots];
   stage_segments(segs, wt);
   const uint32_t n = pb.counts[bounce];
   const bool odd = (bounce & 1) != 0;
@@ -1128,7 +1149,8 @@ __global__ void __launch_bounds__(kShadeThreads) k_shade_nee(PathBatch pb, const
         }
       }
     }
-    const uint32_t slot = block_append_octant(pb.counts + bounce + 1, cont, next_d, append_sh + ((base / stride) & 1u) * 64);
+    const uint32_t slot = block_append_octant<kShadeExtThreads>(
+        pb.counts + bounce + 1, cont, next_d, append_sh + ((base / stride) & 1u) * AppendShape<kShadeExtThreads>::kSlots);
     if (cont) {
       out_o[slot] = next_o;
       out_d[slot] = next_d;
@@ -1259,15 +1281,15 @@ cudaError_t launch_shade(const PathBatch& pb, const WaveTables& wt, uint32_t bou
 
 cudaError_t launch_shade_cache(const PathBatch& pb, const WaveTables& wt, const CacheWave& cw, uint32_t bounce,
                                int sms, cudaStream_t st) {
-  static const int g = blocks_for((const void*)nbd::k_shade_cache, nbd::kShadeThreads, sms);
-  nbd::k_shade_cache<<<g, nbd::kShadeThreads, 0, st>>>(pb, wt, cw, bounce);
+  static const int g = blocks_for((const void*)nbd::k_shade_cache, nbd::kShadeExtThreads, sms);
+  nbd::k_shade_cache<<<g, nbd::kShadeExtThreads, 0, st>>>(pb, wt, cw, bounce);
   return cudaGetLastError();
 }
 
 cudaError_t launch_shade_nee(const PathBatch& pb, const WaveTables& wt, const ShadowQueue& sq, uint32_t bounce,
                              int sms, cudaStream_t st) {
-  static const int g = blocks_for((const void*)nbd::k_shade_nee, nbd::kShadeThreads, sms);
-  nbd::k_shade_nee<<<g, nbd::kShadeThreads, 0, st>>>(pb, wt, sq, bounce);
+  static const int g = blocks_for((const void*)nbd::k_shade_nee, nbd::kShadeExtThreads, sms);
+  nbd::k_shade_nee<<<g, nbd::kShadeExtThreads, 0, st>>>(pb, wt, sq, bounce);
   return cudaGetLastError();
 }
 
