@@ -63,29 +63,33 @@ struct Hit {
 };
 
 // Traversal state of one ray: the world ray, the current ray (world, or instance-local inside
-// a BLAS), the closest hit so far and the depth of the stack both levels share (the stack
-// itself is a separate per-thread array, so that these scalars stay in registers).
+// a BLAS), the distance of the closest hit so far and the depth of the stack both levels share.
+// The stack itself is a separate per-thread array, so that these scalars stay in registers;
+// the rest of the hit record (u, v, triangle, instance), written only when a closer hit is
+// found, lives in two extra slots at the end of that array (kHitSlot), and the world ray's
+// reciprocal direction is recomputed when a BLAS is left - both to keep the state within the
+// register budget of 8 resident blocks of 128 threads.
+constexpr int kHitSlot = kStackSize;  // stack[kHitSlot] = (u, v), stack[kHitSlot + 1] = (tri, inst)
 struct TraceState {
-  V3 wo, wd, winv;
+  V3 wo, wd;
   V3 ro, rd, rinv;
-  Hit h;
+  float t_hit;
   int sp, blas_base;
   uint32_t cur_inst, node, iter, status;
   bool in_blas, have_node;
 };
 
-__device__ __forceinline__ void trace_begin(TraceState& t, const DevScene& s, const V3 wo, const V3 wd) {
-  t.h.t = kNoHit;
-  t.h.u = t.h.v = 0.0f;
-  t.h.tri = 0xFFFFFFFFu;
-  t.h.inst = 0xFFFFFFFFu;
+__device__ __forceinline__ void trace_begin(TraceState& t, uint2* stack, const DevScene& s, const V3 wo,
+                                            const V3 wd) {
+  t.t_hit = kNoHit;
+  stack[kHitSlot] = make_uint2(0u, 0u);
+  stack[kHitSlot + 1] = make_uint2(0xFFFFFFFFu, 0xFFFFFFFFu);
   t.status = 0;
   t.wo = wo;
   t.wd = wd;
-  t.winv = V3{safe_rcp(wd.x), safe_rcp(wd.y), safe_rcp(wd.z)};
   t.ro = wo;
   t.rd = wd;
-  t.rinv = t.winv;
+  t.rinv = V3{safe_rcp(wd.x), safe_rcp(wd.y), safe_rcp(wd.z)};
   t.sp = 0;
   t.blas_base = 0;
   t.in_blas = false;
@@ -105,9 +109,9 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
     return false;
   }
   ++t.iter;
-  const V3 wo = t.wo, wd = t.wd, winv = t.winv;
+  const V3 wo = t.wo, wd = t.wd;
   V3 &ro = t.ro, &rd = t.rd, &rinv = t.rinv;
-  Hit& h = t.h;
+  float& h_t = t.t_hit;
   int &sp = t.sp, &blas_base = t.blas_base;
   bool &in_blas = t.in_blas, &have_node = t.have_node;
   uint32_t &cur_inst = t.cur_inst, &node = t.node, &status = t.status;
@@ -116,7 +120,8 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
     for (;;) {
       if (in_blas && sp == blas_base) {  // BLAS finished: back to the world ray
         in_blas = false;
-        ro = wo; rd = wd; rinv = winv;
+        ro = wo; rd = wd;
+        rinv = V3{safe_rcp(wd.x), safe_rcp(wd.y), safe_rcp(wd.z)};
       }
       if (sp == 0) {
         done = true;
@@ -124,7 +129,7 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
       }
       --sp;
       const uint2 e = stack[sp];
-      if (__uint_as_float(e.y) >= h.t) continue;  // raytracing_sw.wgsl:197,271
+      if (__uint_as_float(e.y) >= h_t) continue;  // raytracing_sw.wgsl:197,271
       if (!in_blas && (e.x & kInstanceBit)) {
         // enter an instance: transform the world ray (raytracing_sw.wgsl:202-206)
         const float4* it = s.inst_trace + 4 * (size_t)(e.x & ~kInstanceBit);
@@ -182,7 +187,7 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
     const float fz = __uint_as_float(__byte_perm(k < 4 ? fz0 : fz1, 0x4B000000u, sel)) - 8388608.0f;
     const float tn = fmaxf(fmaxf(fmaf(nx, ax, bx), fmaf(ny, ay, by)), fmaf(nz, az, bz));
     const float tf = fminf(fminf(fmaf(fx, ax, bx), fmaf(fy, ay, by)), fmaf(fz, az, bz)) * kFarSlack;
-    const bool hit = meta != 0u && tn <= tf && tf >= 0.0f && tn < h.t;
+    const bool hit = meta != 0u && tn <= tf && tf >= 0.0f && tn < h_t;
     key[k] = 0xFFFFFFFFu;
     if (hit) {
       if (in_blas && !(meta & 0x80u)) {
@@ -216,10 +221,10 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
       if (v < 0.0f || u + v > 1.0f) continue;
       const float t = inv_det * dot(e2, q);
       if (t < kBias) continue;
-      if (t < h.t) {
-        h.t = t; h.u = u; h.v = v;
-        h.tri = f2u(b.w);
-        h.inst = cur_inst;
+      if (t < h_t) {
+        h_t = t;
+        stack[kHitSlot] = make_uint2(f2u(u), f2u(v));
+        stack[kHitSlot + 1] = make_uint2(f2u(b.w), cur_inst);
         if (kAny) return false;
       }
     }
@@ -254,7 +259,7 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
     const uint32_t kk = key[k];
     if (kk == 0xFFFFFFFFu) continue;
     const float d = __uint_as_float(kk & ~7u);
-    if (d >= h.t) continue;  // a leaf tested above moved the closest hit
+    if (d >= h_t) continue;  // a leaf tested above moved the closest hit
     const uint32_t slot = kk & 7u;
     const uint32_t meta = ((slot < 4 ? m0 : m1) >> (8 * (slot & 3))) & 0xFFu;
     const uint32_t ref = (meta & 0x80u) ? child_base + (meta & 7u) : (kInstanceBit | (prim_base + (meta & 31u)));
@@ -275,11 +280,16 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
 template <bool kAny>
 __device__ __forceinline__ uint32_t trace_ray(const DevScene& s, const V3 wo, const V3 wd, Hit& h) {
   TraceState t;
-  uint2 stack[kStackSize];
-  trace_begin(t, s, wo, wd);
+  uint2 stack[kStackSize + 2];
+  trace_begin(t, stack, s, wo, wd);
   while (trace_step<kAny>(t, stack, s)) {
   }
-  h = t.h;
+  const uint2 uv = stack[kHitSlot], ti = stack[kHitSlot + 1];
+  h.t = t.t_hit;
+  h.u = __uint_as_float(uv.x);
+  h.v = __uint_as_float(uv.y);
+  h.tri = ti.x;
+  h.inst = ti.y;
   return t.status;
 }
 
