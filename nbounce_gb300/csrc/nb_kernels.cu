@@ -94,8 +94,11 @@ __device__ __forceinline__ void trace_begin(TraceState& t, uint2* stack, const D
   t.blas_base = 0;
   t.in_blas = false;
   t.cur_inst = 0;
-  t.node = 0;                      // the TLAS root
-  t.have_node = s.has_tlas != 0u;  // no TLAS: nothing to hit
+  t.node = 0;  // the TLAS root
+  // no TLAS, or a ray with a NaN or infinite component: nothing to hit (every slab and
+  // triangle comparison of the reference fails on NaN; the box test below relies on it)
+  const float fin = fabsf(wo.x) + fabsf(wo.y) + fabsf(wo.z) + fabsf(wd.x) + fabsf(wd.y) + fabsf(wd.z);
+  t.have_node = s.has_tlas != 0u && fin <= 3.4028235e38f;
   t.iter = 0;
 }
 
@@ -172,6 +175,8 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
   const uint32_t fy0 = pys ? f2u(q4.x) : f2u(q2.z), fy1 = pys ? f2u(q4.y) : f2u(q2.w);
   const uint32_t nz0 = pzs ? f2u(q3.x) : f2u(q4.z), nz1 = pzs ? f2u(q3.y) : f2u(q4.w);
   const uint32_t fz0 = pzs ? f2u(q4.z) : f2u(q3.x), fz1 = pzs ? f2u(q4.w) : f2u(q3.y);
+  // a child is hit when max(tn, 0) <= min(tf, the largest float below the closest hit)
+  const float t_below = __uint_as_float(f2u(h_t) - 1u);  // h_t > 0
   uint32_t key[8];
   uint32_t leaf_mask = 0, n_push = 0;
 #pragma unroll
@@ -187,13 +192,14 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
     const float fz = __uint_as_float(__byte_perm(k < 4 ? fz0 : fz1, 0x4B000000u, sel)) - 8388608.0f;
     const float tn = fmaxf(fmaxf(fmaf(nx, ax, bx), fmaf(ny, ay, by)), fmaf(nz, az, bz));
     const float tf = fminf(fminf(fmaf(fx, ax, bx), fmaf(fy, ay, by)), fmaf(fz, az, bz)) * kFarSlack;
-    const bool hit = meta != 0u && tn <= tf && tf >= 0.0f && tn < h_t;
+    const float lo = fmaxf(tn, 0.0f);
+    const bool hit = meta != 0u && lo <= fminf(tf, t_below);
     key[k] = 0xFFFFFFFFu;
     if (hit) {
       if (in_blas && !(meta & 0x80u)) {
         leaf_mask |= 1u << k;
       } else {
-        key[k] = (f2u(fmaxf(tn, 0.0f)) & ~7u) | (uint32_t)k;
+        key[k] = (f2u(lo) & ~7u) | (uint32_t)k;
         ++n_push;
       }
     }

@@ -136,3 +136,27 @@ def test_axis_aligned_and_surface_origin_rays_match_oracle(soup):
     ties, both = compare_hits(hits, inst, gpu.export()["indices"], rf, ru)
     assert both > 200
     assert np.all(hits[:, 0][hits[:, 0] != NO_HIT] >= 0.1)
+
+
+def test_non_finite_rays_hit_nothing(soup):
+    """Rays with a NaN or infinite origin or direction component meet nothing, as in the
+    oracle (every slab and triangle comparison of the reference fails on NaN); finite rays
+    in the same query are unaffected."""
+    desc, gpu, orc = soup
+    rng = np.random.default_rng(33)
+    n = 512
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, :3] = rng.uniform(-0.5, 0.5, (n, 3)) + np.float32([0.0, 0.0, -3.0])
+    rays[:, 4:7] = rng.normal(0.0, 0.05, (n, 3)) + np.float32([0.0, 0.0, 1.0])
+    bad = np.arange(n) % 2 == 0
+    comp = rng.integers(0, 6, n)
+    vals = np.array([np.nan, np.inf, -np.inf], np.float32)[rng.integers(0, 3, n)]
+    cols = np.where(comp < 3, comp, comp + 1)
+    rays[bad, cols[bad]] = vals[bad]
+    hits, inst = gpu.trace_host(rays)
+    rf, ru, _ = orc.trace(rays)
+    assert np.all(hits[bad, 0] == NO_HIT) and np.all(inst[bad] == 0xFFFFFFFF)
+    assert np.all(rf[bad, 0] == NO_HIT)
+    good = ~bad
+    assert np.sum(rf[good, 0] != NO_HIT) > 25  # 51 of the 256 finite rays meet the soup
+    compare_hits(hits[good], inst[good], gpu.export()["indices"], rf[good], ru[good])
