@@ -103,11 +103,14 @@ typedef struct nb_camera {
 
 /* Environment seen by rays that miss (pathtracing.wgsl:167-170).  The reference samples a
  * BC6H cube map; this ABI takes a constant colour or an equirect RGBA32F map. */
-enum { NB_ENV_CONSTANT = 0, NB_ENV_EQUIRECT = 1 };
+enum { NB_ENV_CONSTANT = 0, NB_ENV_EQUIRECT = 1, NB_ENV_CUBE = 2 };
 typedef struct nb_env_desc {
   uint32_t kind;
   float color[4];          /* NB_ENV_CONSTANT */
-  const float* texels;     /* NB_ENV_EQUIRECT: height rows of width RGBA32F texels (host) */
+  const float* texels;     /* NB_ENV_EQUIRECT: height rows of width RGBA32F texels (host);
+                              NB_ENV_CUBE: 6 faces (+X, -X, +Y, -Y, +Z, -Z: the layer order
+                              of the reference's cube texture, texture.rs:89-144) of height
+                              rows of width texels each, width == height */
   uint32_t width, height;
 } nb_env_desc;
 

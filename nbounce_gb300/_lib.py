@@ -23,6 +23,7 @@ NB_SCENE_DEDUP_MESHES = 1
 NB_SCENE_HOST_ONLY = 2
 NB_ENV_CONSTANT = 0
 NB_ENV_EQUIRECT = 1
+NB_ENV_CUBE = 2
 NB_TRACE_CLOSEST = 0
 NB_TRACE_ANY = 1
 NB_SAMPLE_ENV_NEE = 1

@@ -280,26 +280,34 @@ void nb_scene_destroy(nb_scene* s) {
 }
 
 // ---- environment -----------------------------------------------------------------------
-// Importance-sampling tables of an equirect map: texel weight w = luminance x sin(theta) of
-// the texel row's centre (the solid angle of a texel is proportional to sin(theta)), negative
-// or non-finite luminance counted as 0, a uniform weight if the whole map is black.  Sums in
-// double, tables in float: marginal CDF over rows, a CDF per row, and per texel the density
-// over (u, v) = w / sum(w) x width x height.
+// Importance-sampling tables of an equirect or cube map over its texel table (a cube's six
+// faces stacked, 6 N rows of N texels): texel weight w = luminance x the texel's solid angle
+// at its centre - sin(theta) of the row for an equirect map, 1 / (1 + s^2 + t^2)^(3/2) for a
+// cube face - with negative or non-finite luminance counted as 0 and a uniform luminance if
+// the whole map is black.  Sums in double, tables in float: marginal CDF over rows, a CDF per
+// row, and per texel the density over the table's (u, v) = w / sum(w) x width x height.
 static int build_env_distribution(nb_env* e, const nb_env_desc* desc) {
-  const uint32_t W = desc->width, H = desc->height;
+  const bool cube = desc->kind == NB_ENV_CUBE;
+  const uint32_t W = desc->width, H = cube ? 6 * desc->height : desc->height;
   std::vector<double> w((size_t)W * H), row_sum(H, 0.0);
   double total = 0.0;
   for (int pass = 0; pass < 2 && !(total > 0.0); ++pass) {
     total = 0.0;
     for (uint32_t y = 0; y < H; ++y) {
       const double sin_t = std::sin(3.14159265358979323846 * ((double)y + 0.5) / (double)H);
+      const double tc = 2.0 * ((double)(y % W) + 0.5) / (double)W - 1.0;  // cube: t of the row
       double r = 0.0;
       for (uint32_t x = 0; x < W; ++x) {
         const float* t = desc->texels + ((size_t)y * W + x) * 4;
         double lum = pass == 0 ? 0.2126 * t[0] + 0.7152 * t[1] + 0.0722 * t[2] : 1.0;
         if (!(lum > 0.0) || !std::isfinite(lum)) lum = 0.0;
-        w[(size_t)y * W + x] = lum * sin_t;
-        r += lum * sin_t;
+        double omega = sin_t;
+        if (cube) {
+          const double sc = 2.0 * ((double)x + 0.5) / (double)W - 1.0, j = 1.0 + sc * sc + tc * tc;
+          omega = 1.0 / (j * std::sqrt(j));
+        }
+        w[(size_t)y * W + x] = lum * omega;
+        r += lum * omega;
       }
       row_sum[y] = r;
       total += r;
@@ -336,8 +344,10 @@ static int build_env_distribution(nb_env* e, const nb_env_desc* desc) {
 int nb_env_create(const nb_env_desc* desc, nb_env** out) {
   if (!desc || !out) return fail(NB_ERR_INVALID_ARG, "NULL argument");
   *out = nullptr;
-  if (desc->kind != NB_ENV_CONSTANT && desc->kind != NB_ENV_EQUIRECT)
+  if (desc->kind != NB_ENV_CONSTANT && desc->kind != NB_ENV_EQUIRECT && desc->kind != NB_ENV_CUBE)
     return fail(NB_ERR_INVALID_ARG, "unknown environment kind %u", desc->kind);
+  if (desc->kind == NB_ENV_CUBE && desc->width != desc->height)
+    return fail(NB_ERR_INVALID_ARG, "cube faces must be square (%u x %u)", desc->width, desc->height);
   int st = check_device();
   if (st) return st;
   nb_env* e = new (std::nothrow) nb_env();
@@ -346,19 +356,20 @@ int nb_env_create(const nb_env_desc* desc, nb_env** out) {
   e->dev.r = desc->color[0];
   e->dev.g = desc->color[1];
   e->dev.b = desc->color[2];
-  if (desc->kind == NB_ENV_EQUIRECT) {
+  if (desc->kind == NB_ENV_EQUIRECT || desc->kind == NB_ENV_CUBE) {
     if (!desc->texels || desc->width == 0 || desc->height == 0) {
       delete e;
-      return fail(NB_ERR_INVALID_ARG, "equirect environment needs texels and a size");
+      return fail(NB_ERR_INVALID_ARG, "texel environment needs texels and a size");
     }
-    size_t n = (size_t)desc->width * desc->height * 4 * sizeof(float);
+    const uint32_t rows = desc->kind == NB_ENV_CUBE ? 6 * desc->height : desc->height;
+    size_t n = (size_t)desc->width * rows * 4 * sizeof(float);
     void* p = nullptr;
     if ((st = e->arena.alloc(n, &p))) { delete e; return st; }
     cudaError_t ce = cudaMemcpy(p, desc->texels, n, cudaMemcpyHostToDevice);
     if (ce != cudaSuccess) { e->arena.release(); delete e; return cuda_fail(ce, "cudaMemcpy(env)"); }
     e->dev.texels = (const float4*)p;
     e->dev.width = desc->width;
-    e->dev.height = desc->height;
+    e->dev.height = rows;
     if ((st = build_env_distribution(e, desc))) {
       e->arena.release();
       delete e;

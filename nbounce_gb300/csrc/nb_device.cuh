@@ -129,15 +129,16 @@ struct DevScene {
   uint32_t n_tris, n_inst, n_vertices;
 };
 
-enum EnvKind : uint32_t { kEnvConstant = 0, kEnvEquirect = 1 };
+enum EnvKind : uint32_t { kEnvConstant = 0, kEnvEquirect = 1, kEnvCube = 2 };
 struct DevEnv {
   uint32_t kind;
   float r, g, b;
   const float4* texels;
-  uint32_t width, height;
-  // importance-sampling distribution of an equirect map (piecewise constant over texels,
-  // weight = luminance x sin(theta)): marginal CDF over rows (height + 1), conditional CDFs
-  // per row (height x (width + 1)), density over (u, v) per texel (width x height)
+  uint32_t width, height;  // cube: width = face size, height = 6 x face size (faces stacked)
+  // importance-sampling distribution of an equirect or cube map over its texel rows and
+  // columns (piecewise constant over texels, weight = luminance x the texel's solid angle):
+  // marginal CDF over rows (height + 1), conditional CDFs per row (height x (width + 1)),
+  // density over (u, v) of the whole texel table per texel (width x height)
   const float* cdf_rows;
   const float* cdf_cols;
   const float* pdf_uv;

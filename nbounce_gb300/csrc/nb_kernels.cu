@@ -457,10 +457,61 @@ __global__ void __launch_bounds__(128, 7) k_trace_wave(PathBatch pb, const WaveT
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(ray_total, (unsigned long long)n);
 }
 
-// equirect lookup (the oracle's definition): u = atan2(d.x, -d.z)/(2 pi) + 0.5, v = acos(d.y)/pi
-// of the normalised direction, bilinear with wrap in u and clamp in v; NaN directions see black
+// Cube-map face of a direction and its coordinates s, t in [-1, 1] on that face: the standard
+// cube-map table (Vulkan / D3D, which wgpu's cube textures follow) with faces 0..5 = +X, -X,
+// +Y, -Y, +Z, -Z; the largest magnitude picks the face, ties going to X, then Y.
+__device__ __forceinline__ uint32_t cube_face(V3 d, float* s, float* t) {
+  const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  float sc, tc, ma;
+  uint32_t f;
+  if (ax >= ay && ax >= az) {
+    f = d.x >= 0.0f ? 0u : 1u;
+    ma = ax;
+    sc = d.x >= 0.0f ? -d.z : d.z;
+    tc = -d.y;
+  } else if (ay >= az) {
+    f = d.y >= 0.0f ? 2u : 3u;
+    ma = ay;
+    sc = d.x;
+    tc = d.y >= 0.0f ? d.z : -d.z;
+  } else {
+    f = d.z >= 0.0f ? 4u : 5u;
+    ma = az;
+    sc = d.z >= 0.0f ? d.x : -d.x;
+    tc = -d.y;
+  }
+  *s = sc / ma;
+  *t = tc / ma;
+  return f;
+}
+
+// Environment radiance seen along dir (pathtracing.wgsl:168).
+//  equirect (the oracle's definition): u = atan2(d.x, -d.z)/(2 pi) + 0.5, v = acos(d.y)/pi of the
+//    normalised direction, bilinear with wrap in u and clamp in v;
+//  cube (the reference's texture_cube at mip 0 with a linear clamp-to-edge sampler,
+//    texture.rs:89-144): face and (s, t) by cube_face, texel coordinates ((s + 1) / 2) N - 1/2,
+//    bilinear inside the face with clamp at its edges (GPUs blend across face seams within half
+//    a texel of an edge; this definition does not);
+// NaN (and zero) directions see black.
 __device__ V3 env_lookup(const DevEnv& env, V3 dir) {
   if (env.kind == kEnvConstant) return V3{env.r, env.g, env.b};
+  if (env.kind == kEnvCube) {
+    float s, t;
+    const uint32_t f = cube_face(dir, &s, &t);
+    const int N = (int)env.width;
+    const float fx = (s + 1.0f) * 0.5f * (float)N - 0.5f, fy = (t + 1.0f) * 0.5f * (float)N - 0.5f;
+    if (fx != fx || fy != fy) return V3{0.0f, 0.0f, 0.0f};
+    const float x0 = floorf(fx), y0 = floorf(fy);
+    const float tx = fx - x0, ty = fy - y0;
+    const int xi = (int)x0, yi = (int)y0;
+    const int xa = min(max(xi, 0), N - 1), xb = min(max(xi + 1, 0), N - 1);
+    const int ya = (int)f * N + min(max(yi, 0), N - 1), yb = (int)f * N + min(max(yi + 1, 0), N - 1);
+    const float4 t00 = __ldg(env.texels + (size_t)ya * N + xa), t10 = __ldg(env.texels + (size_t)ya * N + xb);
+    const float4 t01 = __ldg(env.texels + (size_t)yb * N + xa), t11 = __ldg(env.texels + (size_t)yb * N + xb);
+    return V3{(t00.x * (1.0f - tx) + t10.x * tx) * (1.0f - ty) + (t01.x * (1.0f - tx) + t11.x * tx) * ty,
+              (t00.y * (1.0f - tx) + t10.y * tx) * (1.0f - ty) + (t01.y * (1.0f - tx) + t11.y * tx) * ty,
+              (t00.z * (1.0f - tx) + t10.z * tx) * (1.0f - ty) + (t01.z * (1.0f - tx) + t11.z * tx) * ty};
+  }
   V3 d = normalize(dir);
   float u = nb_atan2(d.x, -d.z) * 0.159154943f + 0.5f;
   float v = nb_acos(fminf(fmaxf(d.y, -1.0f), 1.0f)) * 0.318309886f;
@@ -494,9 +545,11 @@ __device__ __forceinline__ uint32_t cdf_index(const float* c, uint32_t n, float 
 }
 
 // Direction of an environment sample for uniform (u1, u2).  Constant environment: uniform on
-// the sphere.  Equirect: texel row by the marginal CDF, column by the row's CDF, uniform
-// inside the texel cell of (u, v), mapped like env_lookup: theta = pi v, phi = 2 pi (u - 1/2),
-// d = (sin theta sin phi, cos theta, -sin theta cos phi).
+// the sphere.  Equirect and cube: texel row by the marginal CDF, column by the row's CDF,
+// uniform inside the texel cell, mapped like env_lookup.  Equirect: theta = pi v,
+// phi = 2 pi (u - 1/2), d = (sin theta sin phi, cos theta, -sin theta cos phi).  Cube: row
+// f N + r of face f, s = 2 (x + du) / N - 1, t = 2 (r + dv) / N - 1, d = the point (s, t) of
+// face f (the inverse of cube_face), normalised.
 __device__ V3 env_sample_dir(const DevEnv& env, float u1, float u2) {
   if (env.kind == kEnvConstant) {
     const float z = 1.0f - 2.0f * u1;
@@ -513,6 +566,20 @@ __device__ V3 env_sample_dir(const DevEnv& env, float u1, float u2) {
   const uint32_t x = cdf_index(row, W + 1, u2);
   const float c0 = __ldg(row + x), c1 = __ldg(row + x + 1);
   const float du = c1 > c0 ? fminf((u2 - c0) / (c1 - c0), 0.99999994f) : 0.5f;
+  if (env.kind == kEnvCube) {
+    const uint32_t f = y / W, r = y - f * W;
+    const float s = 2.0f * (((float)x + du) / (float)W) - 1.0f, t = 2.0f * (((float)r + dv) / (float)W) - 1.0f;
+    V3 d;
+    switch (f) {
+      case 0: d = V3{1.0f, -t, -s}; break;
+      case 1: d = V3{-1.0f, -t, s}; break;
+      case 2: d = V3{s, 1.0f, t}; break;
+      case 3: d = V3{s, -1.0f, -t}; break;
+      case 4: d = V3{s, -t, 1.0f}; break;
+      default: d = V3{-s, -t, -1.0f}; break;
+    }
+    return normalize(d);
+  }
   const float u = ((float)x + du) / (float)W, v = ((float)y + dv) / (float)H;
   float st, ct, sp, cp;
   nb_sincos(kPi * v, &st, &ct);
@@ -521,9 +588,21 @@ __device__ V3 env_sample_dir(const DevEnv& env, float u1, float u2) {
 }
 
 // Solid-angle density with which env_sample_dir produces the unit direction d: 1/(4 pi) for a
-// constant environment; pdf_uv of d's texel / (2 pi^2 sin theta) for an equirect map.
+// constant environment; pdf_uv of d's texel / (2 pi^2 sin theta) for an equirect map; for a
+// cube map pdf_uv of d's texel x (1 + s^2 + t^2)^(3/2) / 24 (the table's v spans 6 faces,
+// (s, t) spans [-1, 1]^2 per face, and d omega = ds dt / (1 + s^2 + t^2)^(3/2)).
 __device__ float env_pdf(const DevEnv& env, V3 d) {
   if (env.kind == kEnvConstant) return 0.0795774715f;
+  if (env.kind == kEnvCube) {
+    float s, t;
+    const uint32_t f = cube_face(d, &s, &t);
+    if (s != s || t != t) return 0.0f;
+    const int N = (int)env.width;
+    const int x = min(max((int)((s + 1.0f) * 0.5f * (float)N), 0), N - 1);
+    const int y = (int)f * N + min(max((int)((t + 1.0f) * 0.5f * (float)N), 0), N - 1);
+    const float j = 1.0f + s * s + t * t;
+    return __ldg(env.pdf_uv + (size_t)y * N + x) * (j * sqrtf(j)) * (1.0f / 24.0f);
+  }
   const float u = nb_atan2(d.x, -d.z) * 0.159154943f + 0.5f;
   const float cy = fminf(fmaxf(d.y, -1.0f), 1.0f);
   const float v = nb_acos(cy) * 0.318309886f;

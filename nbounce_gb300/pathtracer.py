@@ -147,13 +147,22 @@ class SceneBuffers:
 
 
 class EnvMap:
-    """Constant colour or equirect RGBA32F environment on the device."""
+    """Constant colour, equirect RGBA32F (texels: (h, w, 4)) or cube-map RGBA32F (cube:
+    (6, n, n, 4), faces +X, -X, +Y, -Y, +Z, -Z) environment on the device (EnvMap::load,
+    envmap.rs:12)."""
 
-    def __init__(self, color=(0.5, 0.6, 0.8), texels=None):
+    def __init__(self, color=(0.5, 0.6, 0.8), texels=None, cube=None):
         d = L.NbEnvDesc()
         d.color[:] = [float(color[0]), float(color[1]), float(color[2]), 1.0]
         self._tex = None
-        if texels is not None:
+        if cube is not None:
+            self._tex = np.ascontiguousarray(cube, dtype=np.float32)
+            if self._tex.ndim != 4 or self._tex.shape[0] != 6 or self._tex.shape[3] != 4:
+                raise ValueError("cube faces must be (6, n, n, 4)")
+            d.kind = L.NB_ENV_CUBE
+            d.texels = self._tex.ctypes.data
+            d.height, d.width = self._tex.shape[1], self._tex.shape[2]
+        elif texels is not None:
             self._tex = np.ascontiguousarray(texels, dtype=np.float32)
             d.kind = L.NB_ENV_EQUIRECT
             d.texels = self._tex.ctypes.data

@@ -369,6 +369,30 @@ def sky_envmap(seed, width=2048, height=1024, sun_dir=(0.3, 0.8, -0.52), sun_rad
     return out
 
 
+def cube_directions(n):
+    """Unit directions of the texel centres of a cube map with n x n faces: (6, n, n, 3), faces
+    +X, -X, +Y, -Y, +Z, -Z with (s, t) in [-1, 1] per the standard cube-map table."""
+    c = 2.0 * (np.arange(n) + 0.5) / n - 1.0
+    t, s = np.meshgrid(c, c, indexing="ij")
+    one = np.ones_like(s)
+    faces = [np.stack(f, -1) for f in ((one, -t, -s), (-one, -t, s), (s, one, t), (s, -one, -t), (s, -t, one),
+                                       (-s, -t, -one))]
+    d = np.stack(faces)
+    return d / np.linalg.norm(d, axis=-1, keepdims=True)
+
+
+def cube_from_equirect(texels, n):
+    """Cube-map faces (6, n, n, 4) sampled (nearest texel) from an equirect RGBA32F map with the
+    library's equirect mapping u = atan2(x, -z) / 2 pi + 1/2, v = acos(y) / pi."""
+    h, w = texels.shape[:2]
+    d = cube_directions(n)
+    u = np.arctan2(d[..., 0], -d[..., 2]) / (2 * np.pi) + 0.5
+    v = np.arccos(np.clip(d[..., 1], -1.0, 1.0)) / np.pi
+    x = np.clip((u * w).astype(np.int64), 0, w - 1)
+    y = np.clip((v * h).astype(np.int64), 0, h - 1)
+    return np.ascontiguousarray(texels[y, x], dtype=np.float32)
+
+
 def instanced_scene(seed=0x5EED1, n_instances=1024, width=1920, height=1080, spp=64, bounces=8,
                     env_size=(2048, 1024), scale=1.0):
     """16 seeded meshes (50k-1M triangles each, ~4.9M unique) in n_instances instances: one

@@ -421,7 +421,8 @@ typedef struct or_primitive {
 } or_primitive;
 
 typedef struct or_env {
-  uint32_t kind;      // 0 = constant, 1 = equirect RGBA32F
+  uint32_t kind;      // 0 = constant, 1 = equirect RGBA32F, 2 = cube RGBA32F (6 square faces
+                      // +X, -X, +Y, -Y, +Z, -Z of height rows of width texels)
   float color[4];
   const float* texels;
   uint32_t width, height;
@@ -706,8 +707,11 @@ template <class R> static HitInfo<R> intersect_scene(const Scene& sc, const Ray<
 }
 
 // ---------------------------------------------------------------------------------------
-// environment lookup (the reference samples a cube map; the oracle defines a constant and
-// an equirect RGBA32F map, bilinear, clamp in v and wrap in u)
+// environment lookup (pathtracing.wgsl:168 samples a cube texture at mip 0 with a linear
+// clamp-to-edge sampler, texture.rs:89-144).  The oracle defines a constant, an equirect
+// RGBA32F map (bilinear, clamp in v and wrap in u) and a cube map of RGBA32F faces: face and
+// (s, t) by the standard cube-map table (faces +X, -X, +Y, -Y, +Z, -Z; ties to X, then Y),
+// texel coordinates ((s + 1) / 2) N - 1/2, bilinear with clamp at the face's edges.
 // ---------------------------------------------------------------------------------------
 template <class R> static V3<R> env_lookup(const or_env& env, V3<R> dir);
 
@@ -891,6 +895,52 @@ static inline float atan2_f32(float y, float x) {
 }
 static inline float acos_f32(float y) { return atan2_f32(std::sqrt((1.0f - y) * (1.0f + y)), y); }
 
+template <class R> static uint32_t cube_face(R x, R y, R z, R* s, R* t) {
+  const R ax = std::fabs(x), ay = std::fabs(y), az = std::fabs(z);
+  R sc, tc, ma;
+  uint32_t f;
+  if (ax >= ay && ax >= az) {
+    f = x >= R(0) ? 0u : 1u;
+    ma = ax;
+    sc = x >= R(0) ? -z : z;
+    tc = -y;
+  } else if (ay >= az) {
+    f = y >= R(0) ? 2u : 3u;
+    ma = ay;
+    sc = x;
+    tc = y >= R(0) ? z : -z;
+  } else {
+    f = z >= R(0) ? 4u : 5u;
+    ma = az;
+    sc = z >= R(0) ? x : -x;
+    tc = -y;
+  }
+  *s = sc / ma;
+  *t = tc / ma;
+  return f;
+}
+
+template <class R> static V3<R> env_lookup_cube(const or_env& env, V3<R> dir) {
+  R s, t;
+  const uint32_t f = cube_face<R>(dir.x, dir.y, dir.z, &s, &t);
+  const int N = (int)env.width;
+  const R fx = (s + R(1)) * R(0.5) * (R)N - R(0.5), fy = (t + R(1)) * R(0.5) * (R)N - R(0.5);
+  if (fx != fx || fy != fy) return {R(0), R(0), R(0)};
+  const R x0 = std::floor(fx), y0 = std::floor(fy);
+  const R tx = fx - x0, ty = fy - y0;
+  const int xi = (int)x0, yi = (int)y0;
+  const int xa = std::min(std::max(xi, 0), N - 1), xb = std::min(std::max(xi + 1, 0), N - 1);
+  const int ya = (int)f * N + std::min(std::max(yi, 0), N - 1), yb = (int)f * N + std::min(std::max(yi + 1, 0), N - 1);
+  const float* t00 = env.texels + 4 * ((size_t)ya * N + xa);
+  const float* t10 = env.texels + 4 * ((size_t)ya * N + xb);
+  const float* t01 = env.texels + 4 * ((size_t)yb * N + xa);
+  const float* t11 = env.texels + 4 * ((size_t)yb * N + xb);
+  R c[3];
+  for (int ch = 0; ch < 3; ++ch)
+    c[ch] = (R(t00[ch]) * (R(1) - tx) + R(t10[ch]) * tx) * (R(1) - ty) + (R(t01[ch]) * (R(1) - tx) + R(t11[ch]) * tx) * ty;
+  return {c[0], c[1], c[2]};
+}
+
 static V3<float> env_lookup_f32(const or_env& env, V3<float> dir) {
   V3<float> d = normalize(dir);
   float u = atan2_f32(d.x, -d.z) * 0.159154943f + 0.5f;
@@ -915,6 +965,7 @@ static V3<float> env_lookup_f32(const or_env& env, V3<float> dir) {
 
 template <class R> static V3<R> env_lookup(const or_env& env, V3<R> dir) {
   if (env.kind == 0) return {R(env.color[0]), R(env.color[1]), R(env.color[2])};
+  if (env.kind == 2) return env_lookup_cube<R>(env, dir);
   if constexpr (std::is_same<R, float>::value) return env_lookup_f32(env, dir);
   double dx = dir.x, dy = dir.y, dz = dir.z;
   double l = std::sqrt(dx * dx + dy * dy + dz * dz);
@@ -1011,6 +1062,21 @@ void or_hash4u(const uint32_t* in4, uint32_t* out4) { hash4u(in4, out4); }
 void or_hash4f(const uint32_t* in4, float* out4) { hash4f(in4, out4); }
 void or_sincos(const float* x, uint64_t n, float* s, float* c) {
   for (uint64_t i = 0; i < n; ++i) sincos_f32(x[i], &s[i], &c[i]);
+}
+
+// ---- environment lookup (pathtracing.wgsl:168) on caller directions: n x 3 floats in,
+// n x 3 out; precision 32 (binary32, the kernels' contract) or 64 ----
+void or_env_lookup(const or_env* env, const float* dirs, uint64_t n, int precision, float* out) {
+  for (uint64_t i = 0; i < n; ++i) {
+    const float* d = dirs + 3 * i;
+    if (precision == 64) {
+      const V3<double> c = env_lookup<double>(*env, V3<double>{d[0], d[1], d[2]});
+      out[3 * i] = (float)c.x; out[3 * i + 1] = (float)c.y; out[3 * i + 2] = (float)c.z;
+    } else {
+      const V3<float> c = env_lookup<float>(*env, V3<float>{d[0], d[1], d[2]});
+      out[3 * i] = c.x; out[3 * i + 1] = c.y; out[3 * i + 2] = c.z;
+    }
+  }
 }
 
 // ---- Sobol ----

@@ -59,8 +59,38 @@ def lib():
         L.or_render.argtypes = [vp, vp, u32, u32, vp, u64, u32, u32, u32, f32, vp, u32, u32, u32, u32,
                                 vp, vp, i32, i32, vp, vp, u32]
         L.or_render.restype = u64
+        L.or_env_lookup.argtypes = [vp, vp, u64, i32, vp]
         _lib = L
     return _lib
+
+
+def make_env(color=(0.5, 0.6, 0.8), texels=None, cube=None):
+    """OrEnv for a constant colour, an equirect map (h, w, 4) or cube faces (6, n, n, 4);
+    returns (env, the array it points into, which must outlive it)."""
+    e = OrEnv()
+    tex = None
+    if cube is not None:
+        tex = np.ascontiguousarray(cube, dtype=np.float32)
+        e.kind, e.texels = 2, tex.ctypes.data
+        e.height, e.width = tex.shape[1], tex.shape[2]
+    elif texels is not None:
+        tex = np.ascontiguousarray(texels, dtype=np.float32)
+        e.kind, e.texels = 1, tex.ctypes.data
+        e.height, e.width = tex.shape[0], tex.shape[1]
+    else:
+        e.kind = 0
+        e.color[:] = [float(color[0]), float(color[1]), float(color[2]), 1.0]
+    return e, tex
+
+
+def env_lookup(dirs, color=(0.5, 0.6, 0.8), texels=None, cube=None, precision=32):
+    """Environment radiance along directions (n, 3) -> (n, 3) float32."""
+    d = np.ascontiguousarray(dirs, dtype=np.float32).reshape(-1, 3)
+    e, keep = make_env(color, texels, cube)
+    out = np.zeros((d.shape[0], 3), np.float32)
+    lib().or_env_lookup(C.byref(e), _p(d), d.shape[0], precision, _p(out))
+    del keep
+    return out
 
 
 def default_threads():
@@ -160,7 +190,7 @@ class OracleScene:
 
     def render(self, clip_to_world, width, height, sobol, first_sample, spp, bounces=8, contribution_factor=4.0,
                env=(0.5, 0.6, 0.8), region=None, out=None, per_sample=False, precision=32, threads=None,
-               env_texels=None, rr_start=0):
+               env_texels=None, rr_start=0, env_cube=None):
         """Running-mean render of samples first_sample..first_sample+spp-1 (1-based) over a pixel region.
 
         Returns (rgba (h, w, 4) float32, traversal queries, per-sample L (h, w, spp, 4) or None, overflow)."""
@@ -170,16 +200,7 @@ class OracleScene:
         if out is None:
             out = np.zeros((h, w, 4), np.float32)
         ps = np.zeros((h, w, spp, 4), np.float32) if per_sample else None
-        e = OrEnv()
-        if env_texels is not None:
-            tex = np.ascontiguousarray(env_texels, dtype=np.float32)
-            e.kind = 1
-            e.texels = tex.ctypes.data
-            e.height, e.width = tex.shape[0], tex.shape[1]
-        else:
-            tex = None
-            e.kind = 0
-            e.color[:] = [float(env[0]), float(env[1]), float(env[2]), 1.0]
+        e, tex = make_env(env, env_texels, env_cube)
         ovf = C.c_uint32(0)
         self.last_counters = np.zeros(4, np.uint64)
         rays = lib().or_render(self.h, _p(c2w), width, height, _p(sob), sob.size // 4, first_sample, spp, bounces,

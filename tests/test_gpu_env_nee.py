@@ -78,6 +78,62 @@ def test_equirect_sampling_follows_texel_weights():
     assert abs(np.mean(1.0 / pdf[pos]) / (4 * np.pi) - 1) < 0.02
 
 
+def test_cube_sampling_follows_texel_weights():
+    """Cube map: texels of the six stacked faces drawn with probability w / sum(w), w =
+    luminance x 1 / (1 + s^2 + t^2)^(3/2) (the texel's solid angle); density = that
+    probability x 6 n^2 x (1 + s^2 + t^2)^(3/2) / 24 at the direction's own (s, t)."""
+    n = 16
+    rng = np.random.default_rng(4)
+    cube = np.ones((6, n, n, 4), np.float32)
+    cube[..., :3] = np.exp(rng.normal(0.0, 1.0, (6, n, n, 1))) * np.array([1.0, 0.8, 0.6])
+    cube[2, 3, 11, :3] = 400.0  # a bright texel on +Y
+    env = nb.EnvMap(cube=cube)
+    m = 1 << 21
+    smp = sample(env, m, seed=2)
+    d, pdf = smp[:, :3], smp[:, 3]
+    assert np.allclose(np.linalg.norm(d, axis=1), 1.0, atol=1e-5)
+    c = 2.0 * (np.arange(n) + 0.5) / n - 1.0
+    j = 1.0 + c[None, :, None] ** 2 + c[None, None, :] ** 2
+    lum = 0.2126 * cube[..., 0] + 0.7152 * cube[..., 1] + 0.0722 * cube[..., 2]
+    w = lum.astype(np.float64) / (j * np.sqrt(j))
+    P = w / w.sum()
+    # face and texel of each direction (numpy statement of the cube table)
+    a = np.abs(d)
+    f = np.where((a[:, 0] >= a[:, 1]) & (a[:, 0] >= a[:, 2]), np.where(d[:, 0] >= 0, 0, 1),
+                 np.where(a[:, 1] >= a[:, 2], np.where(d[:, 1] >= 0, 2, 3), np.where(d[:, 2] >= 0, 4, 5)))
+    sc = np.choose(f, [-d[:, 2], d[:, 2], d[:, 0], d[:, 0], d[:, 0], -d[:, 0]])
+    tc = np.choose(f, [-d[:, 1], -d[:, 1], d[:, 2], -d[:, 2], -d[:, 1], -d[:, 1]])
+    ma = np.choose(f, [a[:, 0], a[:, 0], a[:, 1], a[:, 1], a[:, 2], a[:, 2]])
+    s_, t_ = sc / ma, tc / ma
+    x = np.clip(((s_ + 1) / 2 * n).astype(int), 0, n - 1)
+    y = np.clip(((t_ + 1) / 2 * n).astype(int), 0, n - 1)
+    hist = np.zeros((6, n, n))
+    np.add.at(hist, (f, y, x), 1.0)
+    tv = 0.5 * np.abs(hist / m - P).sum()
+    assert tv < 0.01, tv
+    jj = 1.0 + s_ ** 2 + t_ ** 2
+    expect = P[f, y, x] * 6 * n * n * jj * np.sqrt(jj) / 24.0
+    assert np.median(np.abs(pdf / expect - 1)) < 1e-3
+    assert np.all(pdf > 0)
+    assert abs(np.mean(1.0 / pdf) / (4 * np.pi) - 1) < 0.02
+
+
+def test_nee_converges_to_plain_cube_sun_sky():
+    """A cube-map sky with a sun: NEE at 2048 spp against plain at 8192 spp."""
+    desc = scenes.spheres_scene(width=48, height=48, bounces=6)
+    tex = scenes.sky_envmap(0x5EED9, 256, 128, sun_diameter_deg=6.0, sun_radiance=200.0)
+    env = nb.EnvMap(cube=scenes.cube_from_equirect(tex, 32))
+    scene = nb.SceneBuffers.from_desc(desc)
+    cam = nb.camera_struct(desc.world_to_clip, desc.clip_to_world)
+    ref = render(desc, scene, env, cam, 8192, False)
+    nee = render(desc, scene, env, cam, 2048, True)
+    m_ref, m_nee = np.nanmean(ref[..., :3]), np.nanmean(nee[..., :3])
+    assert abs(m_nee / m_ref - 1) < 0.01, (m_nee, m_ref)
+    e_plain = rel_mse(render(desc, scene, env, cam, 32, False), ref)
+    e_nee = rel_mse(render(desc, scene, env, cam, 32, True), ref)
+    assert e_nee < e_plain, (e_nee, e_plain)
+
+
 def test_constant_env_sampling_is_uniform():
     env = nb.EnvMap((0.5, 0.6, 0.8))
     s = sample(env, 1 << 20, seed=1)

@@ -108,6 +108,23 @@ def test_equirect_environment_matches_oracle():
     assert rel_mse(img, ref) <= REL_MSE
 
 
+def test_cube_environment_matches_oracle():
+    """NB_ENV_CUBE (the reference's environment type): misses look the cube map up like the
+    oracle - face by the major axis, bilinear inside the face."""
+    desc = scenes.spheres_scene(width=48, height=48, spp=2, bounces=4)
+    cube = scenes.cube_from_equirect(scenes.sky_envmap(3, 256, 128), 24)
+    orc = O.OracleScene(desc.vertices, desc.indices, desc.primitives(), dedup=True)
+    img, _, status, _ = gpu_render(desc, desc.spp, env=nb.EnvMap(cube=cube))
+    ref, _, _, _ = orc.render(desc.clip_to_world, desc.width, desc.height, nb.sobol_burley_table(), 1, desc.spp,
+                              bounces=desc.bounces, env_cube=cube)
+    assert status == 0
+    assert np.mean(np.all(img == ref, axis=-1)) >= EXACT_FRAC
+    assert rel_mse(img, ref) <= REL_MSE
+    plain_sky, _, _, _ = orc.render(desc.clip_to_world, desc.width, desc.height, nb.sobol_burley_table(), 1,
+                                    desc.spp, bounces=desc.bounces, env=desc.env_color)
+    assert not np.array_equal(plain_sky, ref)
+
+
 def test_instanced_scene_crop_matches_oracle():
     desc = scenes.instanced_scene(n_instances=96, width=64, height=36, spp=2, bounces=8, env_size=(256, 128),
                                   scale=1 / 64)
