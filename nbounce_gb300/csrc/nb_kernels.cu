@@ -3,7 +3,8 @@
 // The reference runs one WGSL invocation per pixel that loops over bounces with the whole
 // traversal inline (pathtracing.wgsl:161-260).  Here the pass is a wavefront:
 //   raygen      one path per (pixel, sample) of a batch: Cranley-Patterson-rotated Sobol
-//               jitter and generate_ray (pathtracing.wgsl:27-41, 245-255)
+//               jitter and generate_ray (pathtracing.wgsl:27-41, 245-255), queued in 8x8
+//               pixel tiles
 //   trace       persistent warps take 32 rays at a time with one atomic and walk 8-wide
 //               quantised trees collapsed from the reference's TLAS/BLAS (raytracing_sw.wgsl:
 //               176-319): one 80-byte node load tests eight child boxes, leaf triangles are
@@ -11,7 +12,8 @@
 //               order so the nearest is visited next
 //   shade       hit attributes (raytracing_sw.wgsl:138-173), env/emission termination, lobe
 //               choice, VNDF / cosine sampling, Russian roulette (pathtracing.wgsl:161-241);
-//               survivors are appended to the next bounce's queue with warp-aggregated atomics
+//               each block appends its survivors to the next bounce's queue grouped by
+//               direction octant (one atomic per block)
 //   accumulate  running mean over the batch's samples in sample order (pathtracing.wgsl:258)
 // so traversal runs in a lean kernel and the path state lives in HBM.  A wave can hold paths
 // of several jobs (render requests): tables of segments, jobs and scenes ride in the kernel
@@ -423,8 +425,9 @@ __global__ void __launch_bounds__(256) k_raygen(PathBatch pb, const WaveTables w
 
 // kSingle: every ray of the wave uses wt.scenes[0]; else the scene index carried in q_d.w.
 // Persistent warps take 32 consecutive rays per atomic and trace them together: consecutive
-// queue entries come from neighbouring pixels, so the lanes of a warp walk largely the same
-// nodes (shared cache lines, agreeing branches).  Refilling finished lanes one by one with
+// queue entries come from an 8x4 pixel patch (camera rays) or from one small patch of the
+// image with one direction octant (later bounces), so the lanes of a warp walk largely the
+// same nodes (shared cache lines, agreeing branches).  Refilling finished lanes one by one with
 // unrelated rays, with or without a warp-wide sync per node step, measured 11-30% slower.
 template <bool kSingle>
 __global__ void __launch_bounds__(128, 7) k_trace_wave(PathBatch pb, const WaveTables wt, uint32_t bounce,
