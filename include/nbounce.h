@@ -358,6 +358,12 @@ int nb_server_create(uint64_t hbm_budget_bytes, uint32_t paths_per_wave, nb_serv
 /* Registers a resident scene / environment (the caller keeps them alive until destroy). */
 int nb_server_add_scene(nb_server* server, const nb_scene* scene, uint32_t* slot);
 int nb_server_add_env(nb_server* server, const nb_env* env, uint32_t* slot);
+/* Configuration of the radiance caches the server creates for NB_JOB_CACHE jobs from now on
+ * (NULL: nb_cache_default_config).  It is checked when a scene's cache is created, at its
+ * first cache job; if nb_cache_create rejects it, that scene's queued and active cache jobs
+ * fail with its status and every other job goes on.  Thread-safe. */
+struct nb_cache_config; /* defined with the radiance cache API below */
+int nb_server_set_cache_config(nb_server* server, const struct nb_cache_config* cfg);
 /* Queues a job; thread-safe, returns at once.  NB_ERR_INVALID_ARG for bad slots or sizes,
  * NB_ERR_OOM if the job can never fit the budget. */
 int nb_server_submit(nb_server* server, const nb_job_desc* job, uint64_t* job_id);

@@ -161,6 +161,7 @@ def lib():
         "nb_server_add_scene": ([vp, vp, vp], i32),
         "nb_server_add_env": ([vp, vp, vp], i32),
         "nb_server_submit": ([vp, vp, vp], i32),
+        "nb_server_set_cache_config": ([vp, vp], i32),
         "nb_server_wait": ([vp, u64, i32, vp], i32),
         "nb_server_fetch": ([vp, u64, vp], i32),
         "nb_server_release": ([vp, u64], i32),

@@ -77,6 +77,8 @@ struct nb_server {
   uint64_t fixed_bytes = 0;  // path buffers + tables
   ShadowQueue sq{};          // shadow rays of NB_JOB_ENV_NEE jobs
   std::map<uint32_t, nb_cache*> caches;  // scene slot -> radiance cache of NB_JOB_CACHE jobs
+  nb_cache_config cache_cfg{};
+  bool has_cache_cfg = false;            // else nb_cache_default_config
   bool last_wave_cache = false;
 
   std::vector<const nb_scene*> scenes;
@@ -127,6 +129,32 @@ struct nb_server {
     }
     queue.clear();
     active.clear();
+    cv_done.notify_all();
+  }
+
+  // Fails the unfinished queued or active jobs that `pick` accepts.  Waves of theirs still in
+  // flight run to completion; the images are freed after them (stream order).
+  template <class Pick>
+  void fail_jobs_locked(Pick pick, int status) {
+    auto doomed = [&](Job* j) { return j->state != Job::kDone && pick(j); };
+    for (Job* j : queue)
+      if (doomed(j)) j->state = Job::kDone, j->status = status, j->t_finish = now_ms(), ++jobs_failed;
+    queue.erase(std::remove_if(queue.begin(), queue.end(), [](Job* j) { return j->state == Job::kDone; }),
+                queue.end());
+    for (Job* j : active) {
+      if (!doomed(j)) continue;
+      if (j->d_img) {
+        cudaFreeAsync(j->d_img, stream);
+        j->d_img = nullptr;
+        bytes_in_use -= j->bytes;
+      }
+      j->state = Job::kDone;
+      j->status = status;
+      j->t_finish = now_ms();
+      ++jobs_failed;
+    }
+    active.erase(std::remove_if(active.begin(), active.end(), [](Job* j) { return j->state == Job::kDone; }),
+                 active.end());
     cv_done.notify_all();
   }
 
@@ -270,13 +298,22 @@ struct nb_server {
     return e;
   }
 
-  // a cache wave: the plain prefix kernels with cache-mode shading, lookups and training
-  int launch_cache_wave(uint32_t scene_slot, uint32_t max_bounces) {
+  // the scene's cache (created on first use) and this wave's cache buffers; a failure here
+  // has launched nothing
+  int prepare_cache_wave(uint32_t scene_slot, nb_cache** out, CacheWave* cw) {
     nb_cache*& c = caches[scene_slot];
     int rc = NB_OK;
-    if (!c && (rc = nb_cache_create(nullptr, &c))) return rc;
-    CacheWave cw{};
-    if ((rc = cache_wave_begin(c, scenes[scene_slot], wt->n_paths, &cw, stream))) return rc;
+    if (!c && (rc = nb_cache_create(has_cache_cfg ? &cache_cfg : nullptr, &c))) {
+      c = nullptr;
+      return rc;
+    }
+    *out = c;
+    return cache_wave_begin(c, scenes[scene_slot], wt->n_paths, cw, stream);
+  }
+
+  // a cache wave: the plain prefix kernels with cache-mode shading, lookups and training
+  int launch_cache_wave(nb_cache* c, const CacheWave& cw, uint32_t max_bounces) {
+    int rc = NB_OK;
     PathBatch p = pb;
     cudaError_t e = launch_raygen(p, *wt, sms, stream);
     for (uint32_t b = 0; b <= max_bounces && e == cudaSuccess; ++b) {
@@ -328,7 +365,18 @@ struct nb_server {
           cudaEventRecord(w.start, stream);
           int rc = NB_OK;
           if (want_cache) {
-            rc = launch_cache_wave(cache_scene, max_bounces);
+            nb_cache* c = nullptr;
+            CacheWave cw{};
+            const int setup = prepare_cache_wave(cache_scene, &c, &cw);
+            if (setup != NB_OK) {  // the scene's cache jobs fail; the other jobs go on
+              fail_jobs_locked([&](const Job* j) { return (j->desc.flags & NB_JOB_CACHE) && j->desc.scene == cache_scene; },
+                               setup);
+              event_pool.push_back(w.start);
+              event_pool.push_back(w.stop);
+              last_wave_cache = true;
+              continue;
+            }
+            rc = launch_cache_wave(c, cw, max_bounces);
           } else {
             cudaError_t e = launch_wave(max_bounces, single, nee);
             if (e != cudaSuccess) rc = cuda_fail(e, "wave launch");
@@ -360,6 +408,7 @@ struct nb_server {
         }
         gpu_busy_ms += ms;
         for (Job* j : w.jobs) {
+          if (j->state == Job::kDone) continue;  // failed while this wave ran
           j->finished_waves += 1;
           if (j->fully_planned && j->finished_waves == j->planned_waves) complete_locked(j);
         }
@@ -461,6 +510,14 @@ int nb_server_add_env(nb_server* s, const nb_env* env, uint32_t* slot) {
   std::lock_guard<std::mutex> lk(s->mu);
   *slot = (uint32_t)s->envs.size();
   s->envs.push_back(env);
+  return NB_OK;
+}
+
+int nb_server_set_cache_config(nb_server* s, const struct nb_cache_config* cfg) {
+  if (!s) return fail(NB_ERR_INVALID_ARG, "NULL argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->has_cache_cfg = cfg != nullptr;
+  if (cfg) s->cache_cfg = *cfg;
   return NB_OK;
 }
 

@@ -53,6 +53,17 @@ class RenderServer:
         check(lib().nb_server_submit(self._h, C.byref(d), C.byref(jid)))
         return jid.value
 
+    def set_cache_config(self, **fields):
+        """Configuration of the radiance caches created from now on for NB_JOB_CACHE jobs:
+        nb_cache_default_config with the given fields replaced (no fields: the defaults)."""
+        cfg = L.NbCacheConfig()
+        lib().nb_cache_default_config(C.byref(cfg))
+        for k, v in fields.items():
+            if not hasattr(cfg, k):
+                raise AttributeError(f"nb_cache_config has no field {k!r}")
+            setattr(cfg, k, v)
+        check(lib().nb_server_set_cache_config(self._h, C.byref(cfg) if fields else None))
+
     def wait(self, job, timeout_ms=-1):
         info = L.NbJobInfo()
         st = lib().nb_server_wait(self._h, job, int(timeout_ms), C.byref(info))

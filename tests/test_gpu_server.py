@@ -172,3 +172,38 @@ def test_job_flags_are_validated(world):
             srv.submit(slot, env, w2c, c2w, 32, 32, 1, flags=bad)
         assert e.value.status == 1
     srv.close()
+
+
+def test_rejected_cache_config_fails_only_the_cache_jobs(world):
+    """A cache configuration nb_cache_create rejects is found when the scene's cache is
+    created: that scene's cache jobs fail with its status, every other job completes with its
+    usual image, and a later valid configuration serves new cache jobs."""
+    paths = 1 << 14
+    srv = RenderServer(hbm_budget_bytes=1 << 30, paths_per_wave=paths)
+    slots = [srv.add_scene(s) for s in world["scenes"]]
+    env_slots = [srv.add_env(e) for e in world["envs"]]
+    srv.set_cache_config(train_steps=1000)  # above the 64 steps a cache accepts
+    flags = [L.NB_JOB_CACHE if i in (1, 3) else 0 for i in range(len(JOBS))]  # both on scene 1
+    outs = [np.full((h, w, 4), np.nan, np.float32) for (_, w, h, _, _) in JOBS]
+    ids = []
+    for (k, w, h, spp, b), out, f in zip(JOBS, outs, flags):
+        w2c, c2w = scenes.camera_matrices(*CAMS[k], w, h)
+        ids.append(srv.submit(slots[k], env_slots[k], w2c, c2w, w, h, spp, b, out=out, flags=f))
+    for jid, (k, w, h, spp, b), out, f in zip(ids, JOBS, outs, flags):
+        if f:
+            with pytest.raises(nb.NbError) as e:
+                srv.wait(jid, timeout_ms=120000)
+            assert e.value.status == 1
+        else:
+            info = srv.wait(jid, timeout_ms=120000)
+            assert info["done"] == 1 and info["status"] == 0
+            assert np.array_equal(out, alone(world, k, w, h, spp, b)), (k, w, h, spp, b)
+    assert srv.stats()["jobs_failed"] == 2
+    srv.set_cache_config(tensor_path=L.NB_CACHE_MMA_SYNC)
+    k, w, h, spp, b = JOBS[1]
+    w2c, c2w = scenes.camera_matrices(*CAMS[k], w, h)
+    out = np.full((h, w, 4), np.nan, np.float32)
+    jid = srv.submit(slots[k], env_slots[k], w2c, c2w, w, h, spp, b, out=out, flags=L.NB_JOB_CACHE)
+    info = srv.wait(jid, timeout_ms=120000)
+    assert info["status"] == 0 and np.isfinite(out).all() and (out[..., 3] == 1.0).all()
+    srv.close()
