@@ -63,6 +63,9 @@ def parse():
     p.add_argument("--serving-loads", type=str, default="10:60,30:90,60:120",
                    help="rate:jobs pairs of Poisson loads for the serving report")
     p.add_argument("--no-cache", action="store_true", help="skip the radiance-cache report")
+    p.add_argument("--env-nee", action="store_true",
+                   help="time the opt-in environment-NEE estimator instead of the reference's (rays counted "
+                        "are the closest-hit queries; no CPU baseline or roofline: the oracle has no NEE)")
     p.add_argument("--all-configs", action="store_true",
                    help="instead of the benchmark line, measure the other workloads (spheres 256x256 16 spp, "
                         "1M-triangle soup traversal) on GPU and CPU and print them as one JSON line")
@@ -468,6 +471,8 @@ def run_ours(args):
     pt = nb.Pathtracer(desc.width, desc.height, nb.Globals(bounces=desc.bounces))
     if args.batch_paths:
         pt.set_batch_paths(args.batch_paths)
+    if args.env_nee:
+        pt.set_sampling(env_nee=True)
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
 
@@ -536,7 +541,8 @@ def run_ours(args):
                    "instanced_triangles": int(desc.n_triangles_instanced), "instances": len(desc.instances),
                    "rays_per_step": int(rays_per_step), "parallelism": f"replicas x{world}",
                    "l2": "inputs larger than L2 (scene ~0.8 GB + path queues), no flush",
-                   "scene_build_s": round(build_s, 2)},
+                   "scene_build_s": round(build_s, 2),
+                   "estimator": "environment NEE (opt-in)" if args.env_nee else "reference"},
         "e2e": {"value": round(e2e_value, 2), "unit": UNIT, "h2d_bytes_per_step": 128,
                 "d2h_bytes_per_step": int(desc.width * desc.height * 16)},
         "gpu_launches": int(round(launches_per_step * args.steps)),
@@ -551,7 +557,7 @@ def run_ours(args):
         line["cache"] = cache_report(args, desc, scene, env, stream)
     peak, peak_kind = measured_peaks()
     sobol = nb.sobol_burley_table()
-    if not args.no_cpu_baseline:
+    if not args.no_cpu_baseline and not args.env_nee:
         base, per_ray, _ = cpu_baseline(desc, sobol, args.cpu_seconds, os.cpu_count() or 1)
         line["cpu_baseline"] = base
         n_aabb, n_tri, n_inst = per_ray
