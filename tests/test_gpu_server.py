@@ -207,3 +207,40 @@ def test_rejected_cache_config_fails_only_the_cache_jobs(world):
     info = srv.wait(jid, timeout_ms=120000)
     assert info["status"] == 0 and np.isfinite(out).all() and (out[..., 3] == 1.0).all()
     srv.close()
+
+
+def test_concurrent_submitters_get_their_own_images(world):
+    """nb_server_submit / _wait are thread-safe: four host threads submit and wait at the same
+    time; every job ends with the image of the same job rendered alone."""
+    import threading
+    paths = 1 << 14
+    srv = RenderServer(hbm_budget_bytes=1 << 30, paths_per_wave=paths)
+    slots = [srv.add_scene(s) for s in world["scenes"]]
+    env_slots = [srv.add_env(e) for e in world["envs"]]
+    results, errors = {}, []
+
+    def worker(t):
+        try:
+            for n in range(3):
+                k, w, h, spp, b = JOBS[(t + 2 * n) % len(JOBS)]
+                w2c, c2w = scenes.camera_matrices(*CAMS[k], w, h)
+                out = np.full((h, w, 4), np.nan, np.float32)
+                jid = srv.submit(slots[k], env_slots[k], w2c, c2w, w, h, spp, b, out=out,
+                                 flags=L.NB_JOB_ENV_NEE if (t + n) % 3 == 0 else 0)
+                info = srv.wait(jid, timeout_ms=120000)
+                results[(t, n)] = (info, out, (k, w, h, spp, b), (t + n) % 3 == 0)
+        except Exception as e:  # surfaced below
+            errors.append(e)
+
+    threads = [threading.Thread(target=worker, args=(t,)) for t in range(4)]
+    for th in threads:
+        th.start()
+    for th in threads:
+        th.join()
+    assert not errors, errors
+    assert len(results) == 12
+    for info, out, job, nee in results.values():
+        assert info["done"] == 1 and info["status"] == 0
+        assert np.array_equal(out, alone(world, *job, env_nee=nee)), job
+    assert srv.stats()["jobs_done"] == 12
+    srv.close()
