@@ -788,6 +788,103 @@ void instance_box(const nb_instance& in, const nb_bvh_node& r, float* box) {
   for (int q = 0; q < 3; ++q) { box[q] = wmn[q]; box[3 + q] = wmx[q]; }
 }
 
+// World boxes of the instances for the device TLAS: the bounds of the instance's BLAS
+// vertices transformed by local_to_world in double, widened by 1e-5 of the box's largest
+// extent plus 1e-6 of its coordinates' magnitude (the rounding of the binary32 transforms on
+// either side is ~1e-7 relative) and rounded outward to float.  For a rotated instance this
+// is much tighter than the box of its transformed BLAS root box, which the reference builds
+// its TLAS over (a rotated box's corners reach up to sqrt(3) times further out per axis than
+// a round mesh inside it).  Traversal stays conservative: every box contains its instance's
+// geometry.  An instance whose BLAS has no vertices keeps the transformed root box.
+void tight_instance_boxes(const HostScene& s, std::vector<float>* box) {
+  const size_t n_inst = s.instances.size();
+  std::map<uint32_t, std::vector<uint32_t>> verts;  // BLAS root -> its vertices (sorted, unique)
+  for (const nb_instance& in : s.instances) {
+    if (verts.count(in.node)) continue;
+    std::vector<uint32_t> v, st{in.node};
+    while (!st.empty()) {
+      const nb_bvh_node& b = s.blas[st.back()];
+      st.pop_back();
+      if (b.end > 0) {
+        for (uint32_t t = b.start; t < b.end; ++t)
+          for (int k = 0; k < 3; ++k) v.push_back(s.indices[3 * (size_t)t + k]);
+      } else {
+        st.push_back(b.start);
+        st.push_back(b.start + 1);
+      }
+    }
+    std::sort(v.begin(), v.end());
+    v.erase(std::unique(v.begin(), v.end()), v.end());
+    verts.emplace(in.node, std::move(v));
+  }
+  box->assign(6 * n_inst, 0.0f);
+  auto one = [&](size_t i) {
+    const nb_instance& in = s.instances[i];
+    float* out = box->data() + 6 * i;
+    const std::vector<uint32_t>& v = verts.at(in.node);
+    if (v.empty()) {
+      instance_box(in, s.blas[in.node], out);
+      return;
+    }
+    const float* m = in.local_to_world;
+    double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
+    for (uint32_t vi : v) {
+      const float* p = s.vertices[vi].position;
+      for (int r = 0; r < 3; ++r) {
+        const double w = (double)m[r] * p[0] + (double)m[4 + r] * p[1] + (double)m[8 + r] * p[2] + (double)m[12 + r];
+        lo[r] = std::min(lo[r], w);
+        hi[r] = std::max(hi[r], w);
+      }
+    }
+    const double ext = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
+    for (int r = 0; r < 3; ++r) {
+      const double mag = std::max(std::fabs(lo[r]), std::fabs(hi[r]));
+      const double pad = 1e-5 * ext + 1e-6 * mag;
+      out[r] = std::nextafter((float)(lo[r] - pad), -INFINITY);
+      out[3 + r] = std::nextafter((float)(hi[r] + pad), INFINITY);
+    }
+  };
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  std::atomic<size_t> next{0};
+  std::vector<std::thread> pool;
+  for (unsigned w = 0; w < hw; ++w)
+    pool.emplace_back([&] {
+      for (size_t i; (i = next.fetch_add(1)) < n_inst;) one(i);
+    });
+  for (std::thread& th : pool) th.join();
+}
+
+// The reference TLAS topology with every box recomputed from the instances' (tight) boxes:
+// leaves bound their instances, inner nodes their two children.
+std::vector<nb_bvh_node> refit_tlas(const std::vector<nb_bvh_node>& tlas, const std::vector<float>& ibox) {
+  std::vector<nb_bvh_node> t = tlas;
+  std::vector<std::pair<uint32_t, bool>> st{{0u, false}};
+  while (!st.empty()) {
+    const auto [n, children_done] = st.back();
+    st.pop_back();
+    nb_bvh_node& b = t[n];
+    if (b.end > 0) {
+      for (int k = 0; k < 3; ++k) { b.min[k] = INFINITY; b.max[k] = -INFINITY; }
+      for (uint32_t i = b.start; i < b.end; ++i)
+        for (int k = 0; k < 3; ++k) {
+          b.min[k] = std::min(b.min[k], ibox[6 * (size_t)i + k]);
+          b.max[k] = std::max(b.max[k], ibox[6 * (size_t)i + 3 + k]);
+        }
+    } else if (!children_done) {
+      st.push_back({n, true});
+      st.push_back({b.start, false});
+      st.push_back({b.start + 1, false});
+    } else {
+      const nb_bvh_node &l = t[b.start], &h = t[b.start + 1];
+      for (int k = 0; k < 3; ++k) {
+        b.min[k] = std::min(l.min[k], h.min[k]);
+        b.max[k] = std::max(l.max[k], h.max[k]);
+      }
+    }
+  }
+  return t;
+}
+
 }  // namespace
 
 int to_device_layout(HostScene* s) {
@@ -846,9 +943,10 @@ int to_device_layout(HostScene* s) {
   if (s->has_tlas) {
     int st = check_tree(s->tlas, 0, n_inst);
     if (st) return st;
-    std::vector<float> ibox(6 * n_inst);
-    for (size_t i = 0; i < n_inst; ++i) instance_box(s->instances[i], s->blas[s->instances[i].node], &ibox[6 * i]);
-    Collapser ct{s->tlas, ibox, &s->wtlas, &inst_order, 1};
+    std::vector<float> ibox;
+    tight_instance_boxes(*s, &ibox);
+    const std::vector<nb_bvh_node> tlas = refit_tlas(s->tlas, ibox);
+    Collapser ct{tlas, ibox, &s->wtlas, &inst_order, 1};
     ct.build(0);  // raytracing_sw.wgsl:183-186: the TLAS root is node 0
   }
   s->itrace.assign(inst_order.size(), GpuInstTrace{});
