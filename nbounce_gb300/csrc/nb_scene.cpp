@@ -12,6 +12,10 @@
 // into private node lists that are concatenated in primitive order with their indices
 // offset, and large subtrees inside one BLAS are split on separate threads, after which the
 // reference's node numbering is replayed (append_tree_parallel).
+//
+// The device trees (to_device_layout) are the reference BLAS trees collapsed to 8-wide nodes,
+// and a device TLAS of our own over tight world boxes of instances and of the parts of large
+// instances (tlas_entries, entry_boxes); the reference TLAS itself is kept for export.
 
 #include <algorithm>
 #include <atomic>
@@ -496,9 +500,9 @@ namespace {
 // (1 to 3 triangles, with a triangle-test weight) was 0.3-1.5% slower than fixed 2-triangle
 // leaves.  Nodes are emitted breadth-first so the inner children of a node are contiguous,
 // and the primitives of a node's leaf slots are written contiguously, in slot order, into a
-// new primitive order.  Traversal finds the same closest hit: the wide tree covers the same
-// primitives with boxes that contain the reference boxes; only the visiting order (exact-t
-// ties) can differ.
+// new primitive order.  Traversal finds the same closest hit: the wide BLAS trees cover the
+// same triangles with boxes that contain the reference boxes, and the device TLAS covers every
+// instance's geometry; only the visiting order (exact-t ties) can differ.
 // ---------------------------------------------------------------------------------------
 struct Item {
   bool inner;       // inner binary node (else: primitive range)
@@ -788,60 +792,107 @@ void instance_box(const nb_instance& in, const nb_bvh_node& r, float* box) {
   for (int q = 0; q < 3; ++q) { box[q] = wmn[q]; box[3 + q] = wmx[q]; }
 }
 
-// World boxes of the instances for the device TLAS: the bounds of the instance's BLAS
-// vertices transformed by local_to_world in double, widened by 1e-5 of the box's largest
-// extent plus 1e-6 of its coordinates' magnitude (the rounding of the binary32 transforms on
-// either side is ~1e-7 relative) and rounded outward to float.  For a rotated instance this
-// is much tighter than the box of its transformed BLAS root box, which the reference builds
-// its TLAS over (a rotated box's corners reach up to sqrt(3) times further out per axis than
-// a round mesh inside it).  Traversal stays conservative: every box contains its instance's
-// geometry.  An instance whose BLAS has no vertices keeps the transformed root box.
-void tight_instance_boxes(const HostScene& s, std::vector<float>* box) {
-  const size_t n_inst = s.instances.size();
-  std::map<uint32_t, std::vector<uint32_t>> verts;  // BLAS root -> its vertices (sorted, unique)
-  for (const nb_instance& in : s.instances) {
-    if (verts.count(in.node)) continue;
-    std::vector<uint32_t> v, st{in.node};
+// Entries of the device TLAS: an instance and the wide BLAS node its traversal starts at.
+// An instance whose world box (the transformed BLAS root box the reference builds its TLAS
+// over) has more than kRebraidArea of the scene's box area, and whose BLAS root has only
+// inner children, enters once per child (partial re-braiding, Benthin et al. 2017, "Improved
+// two-level BVHs using partial re-braiding"): the TLAS can then cull the parts of a large
+// instance - the benchmark scene's terrain - that a ray misses, while small instances, for
+// which a second entry would only repeat the ray transform, enter once.  Measured on the
+// benchmark frame: 1452 -> 1518 Mrays/s; splitting every instance whose root has only inner
+// children: 1409.
+constexpr double kRebraidArea = 0.02;
+struct TlasEntry {
+  uint32_t inst, node;
+};
+
+std::vector<TlasEntry> tlas_entries(const HostScene& s, const std::vector<uint32_t>& inst_blas) {
+  auto area = [](const float* lo, const float* hi) {
+    const double x = (double)hi[0] - lo[0], y = (double)hi[1] - lo[1], z = (double)hi[2] - lo[2];
+    return x * y + x * z + y * z;
+  };
+  const double scene = area(s.tlas[0].min, s.tlas[0].max);
+  std::vector<TlasEntry> e;
+  for (size_t i = 0; i < s.instances.size(); ++i) {
+    const uint32_t root = s.wblas_root[inst_blas[i]];
+    const WideNode& w = s.wblas[root];
+    bool split = w.n_children > 1;
+    for (int k = 0; k < w.n_children; ++k) split = split && (w.meta[k] & 0x80u);
+    if (split) {
+      float ib[6];
+      instance_box(s.instances[i], s.blas[s.instances[i].node], ib);
+      split = area(ib, ib + 3) > kRebraidArea * scene;
+    }
+    if (split) {
+      for (int k = 0; k < w.n_children; ++k) e.push_back({(uint32_t)i, w.child_base + (w.meta[k] & 7u)});
+    } else {
+      e.push_back({(uint32_t)i, root});
+    }
+  }
+  return e;
+}
+
+// World boxes of the TLAS entries: the bounds of the vertices below the entry's wide node
+// under the instance's local_to_world, in double, widened by 1e-5 of the box's largest
+// extent plus 1e-6 of its coordinates' magnitude (the binary32 transforms on either side
+// round at ~1e-7 relative) and rounded outward to float.  For a rotated instance this is much
+// tighter than the box of its transformed BLAS root box (a rotated box's corners reach up to
+// sqrt(3) times further out per axis than a round mesh inside it: 1357 -> 1452 Mrays/s on the
+// benchmark frame).  Traversal stays conservative: every box contains its entry's geometry.
+void entry_boxes(const HostScene& s, const std::vector<uint32_t>& tri_order, const std::vector<TlasEntry>& e,
+                 std::vector<Prim>* out) {
+  std::map<uint32_t, std::vector<uint32_t>> verts;  // wide node -> vertices below it (sorted, unique)
+  for (const TlasEntry& en : e) {
+    if (verts.count(en.node)) continue;
+    std::vector<uint32_t> v, st{en.node};
     while (!st.empty()) {
-      const nb_bvh_node& b = s.blas[st.back()];
+      const WideNode& w = s.wblas[st.back()];
       st.pop_back();
-      if (b.end > 0) {
-        for (uint32_t t = b.start; t < b.end; ++t)
-          for (int k = 0; k < 3; ++k) v.push_back(s.indices[3 * (size_t)t + k]);
-      } else {
-        st.push_back(b.start);
-        st.push_back(b.start + 1);
+      for (int k = 0; k < w.n_children; ++k) {
+        const uint32_t meta = w.meta[k];
+        if (meta & 0x80u) {
+          st.push_back(w.child_base + (meta & 7u));
+          continue;
+        }
+        const uint32_t first = w.prim_base + (meta & 31u), cnt = meta >> 5;
+        for (uint32_t j = 0; j < cnt; ++j) {
+          const uint32_t t = tri_order[first + j];
+          for (int q = 0; q < 3; ++q) v.push_back(s.indices[3 * (size_t)t + q]);
+        }
       }
     }
     std::sort(v.begin(), v.end());
     v.erase(std::unique(v.begin(), v.end()), v.end());
-    verts.emplace(in.node, std::move(v));
+    verts.emplace(en.node, std::move(v));
   }
-  box->assign(6 * n_inst, 0.0f);
-  auto one = [&](size_t i) {
-    const nb_instance& in = s.instances[i];
-    float* out = box->data() + 6 * i;
-    const std::vector<uint32_t>& v = verts.at(in.node);
-    if (v.empty()) {
-      instance_box(in, s.blas[in.node], out);
+  out->assign(e.size(), Prim{});
+  auto one = [&](size_t j) {
+    const nb_instance& in = s.instances[e[j].inst];
+    const std::vector<uint32_t>& v = verts.at(e[j].node);
+    Prim& p = (*out)[j];
+    p.payload = (uint32_t)j;
+    if (v.empty()) {  // no geometry: the transformed root box
+      float ib[6];
+      instance_box(in, s.blas[in.node], ib);
+      for (int r = 0; r < 3; ++r) { p.mn[r] = ib[r]; p.mx[r] = ib[3 + r]; p.c[r] = (p.mn[r] + p.mx[r]) * 0.5f; }
       return;
     }
     const float* m = in.local_to_world;
     double lo[3] = {INFINITY, INFINITY, INFINITY}, hi[3] = {-INFINITY, -INFINITY, -INFINITY};
     for (uint32_t vi : v) {
-      const float* p = s.vertices[vi].position;
+      const float* q = s.vertices[vi].position;
       for (int r = 0; r < 3; ++r) {
-        const double w = (double)m[r] * p[0] + (double)m[4 + r] * p[1] + (double)m[8 + r] * p[2] + (double)m[12 + r];
+        const double w = (double)m[r] * q[0] + (double)m[4 + r] * q[1] + (double)m[8 + r] * q[2] + (double)m[12 + r];
         lo[r] = std::min(lo[r], w);
         hi[r] = std::max(hi[r], w);
       }
     }
     const double ext = std::max(hi[0] - lo[0], std::max(hi[1] - lo[1], hi[2] - lo[2]));
     for (int r = 0; r < 3; ++r) {
-      const double mag = std::max(std::fabs(lo[r]), std::fabs(hi[r]));
-      const double pad = 1e-5 * ext + 1e-6 * mag;
-      out[r] = std::nextafter((float)(lo[r] - pad), -INFINITY);
-      out[3 + r] = std::nextafter((float)(hi[r] + pad), INFINITY);
+      const double pad = 1e-5 * ext + 1e-6 * std::max(std::fabs(lo[r]), std::fabs(hi[r]));
+      p.mn[r] = std::nextafter((float)(lo[r] - pad), -INFINITY);
+      p.mx[r] = std::nextafter((float)(hi[r] + pad), INFINITY);
+      p.c[r] = (p.mn[r] + p.mx[r]) * 0.5f;
     }
   };
   const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
@@ -849,40 +900,9 @@ void tight_instance_boxes(const HostScene& s, std::vector<float>* box) {
   std::vector<std::thread> pool;
   for (unsigned w = 0; w < hw; ++w)
     pool.emplace_back([&] {
-      for (size_t i; (i = next.fetch_add(1)) < n_inst;) one(i);
+      for (size_t j; (j = next.fetch_add(1)) < e.size();) one(j);
     });
   for (std::thread& th : pool) th.join();
-}
-
-// The reference TLAS topology with every box recomputed from the instances' (tight) boxes:
-// leaves bound their instances, inner nodes their two children.
-std::vector<nb_bvh_node> refit_tlas(const std::vector<nb_bvh_node>& tlas, const std::vector<float>& ibox) {
-  std::vector<nb_bvh_node> t = tlas;
-  std::vector<std::pair<uint32_t, bool>> st{{0u, false}};
-  while (!st.empty()) {
-    const auto [n, children_done] = st.back();
-    st.pop_back();
-    nb_bvh_node& b = t[n];
-    if (b.end > 0) {
-      for (int k = 0; k < 3; ++k) { b.min[k] = INFINITY; b.max[k] = -INFINITY; }
-      for (uint32_t i = b.start; i < b.end; ++i)
-        for (int k = 0; k < 3; ++k) {
-          b.min[k] = std::min(b.min[k], ibox[6 * (size_t)i + k]);
-          b.max[k] = std::max(b.max[k], ibox[6 * (size_t)i + 3 + k]);
-        }
-    } else if (!children_done) {
-      st.push_back({n, true});
-      st.push_back({b.start, false});
-      st.push_back({b.start + 1, false});
-    } else {
-      const nb_bvh_node &l = t[b.start], &h = t[b.start + 1];
-      for (int k = 0; k < 3; ++k) {
-        b.min[k] = std::min(l.min[k], h.min[k]);
-        b.max[k] = std::max(l.max[k], h.max[k]);
-      }
-    }
-  }
-  return t;
 }
 
 }  // namespace
@@ -934,30 +954,36 @@ int to_device_layout(HostScene* s) {
     g.pad = 0.0f;
   }
 
-  // TLAS over instances (boxes from their BLAS roots), instances re-ordered by the wide TLAS
+  // TLAS over the entries (tlas_entries, entry_boxes): the reference's SAH build over their
+  // boxes, collapsed like the BLAS; entries re-ordered by the wide TLAS
   s->wtlas.clear();
   s->itrace.clear();
   s->ishade.assign(n_inst, GpuInstShade{});
   s->has_tlas = !s->tlas.empty() && n_inst > 0;
-  std::vector<uint32_t> inst_order;
   if (s->has_tlas) {
     int st = check_tree(s->tlas, 0, n_inst);
     if (st) return st;
-    std::vector<float> ibox;
-    tight_instance_boxes(*s, &ibox);
-    const std::vector<nb_bvh_node> tlas = refit_tlas(s->tlas, ibox);
-    Collapser ct{tlas, ibox, &s->wtlas, &inst_order, 1};
+    const std::vector<TlasEntry> entries = tlas_entries(*s, inst_blas);
+    std::vector<Prim> eb;
+    entry_boxes(*s, tri_order, entries, &eb);
+    std::vector<nb_bvh_node> tlas;
+    append_tree(tlas, eb.data(), 0, (uint32_t)eb.size());
+    std::vector<float> ebox(6 * eb.size());
+    for (size_t k = 0; k < eb.size(); ++k)
+      for (int q = 0; q < 3; ++q) { ebox[6 * k + q] = eb[k].mn[q]; ebox[6 * k + 3 + q] = eb[k].mx[q]; }
+    std::vector<uint32_t> order;
+    Collapser ct{tlas, ebox, &s->wtlas, &order, 1};
     ct.build(0);  // raytracing_sw.wgsl:183-186: the TLAS root is node 0
-  }
-  s->itrace.assign(inst_order.size(), GpuInstTrace{});
-  for (size_t k = 0; k < inst_order.size(); ++k) {
-    const uint32_t i = inst_order[k];
-    const nb_instance& in = s->instances[i];
-    GpuInstTrace& tr = s->itrace[k];
-    for (int r = 0; r < 3; ++r)
-      for (int c = 0; c < 4; ++c) tr.row[r][c] = in.world_to_local[4 * c + r];
-    tr.blas_root = s->wblas_root[inst_blas[i]];
-    tr.ref_index = i;
+    s->itrace.assign(order.size(), GpuInstTrace{});
+    for (size_t k = 0; k < order.size(); ++k) {
+      const TlasEntry& en = entries[eb[order[k]].payload];
+      const nb_instance& in = s->instances[en.inst];
+      GpuInstTrace& tr = s->itrace[k];
+      for (int r = 0; r < 3; ++r)
+        for (int c = 0; c < 4; ++c) tr.row[r][c] = in.world_to_local[4 * c + r];
+      tr.blas_root = en.node;
+      tr.ref_index = en.inst;
+    }
   }
   for (size_t i = 0; i < n_inst; ++i) {
     const nb_instance& in = s->instances[i];
