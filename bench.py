@@ -40,9 +40,9 @@ if ROOT not in sys.path:
 
 METRIC = "Mrays/s (primary + extension rays), 1920x1080 64spp 8 bounces"
 # DRAM bytes (read + write) per traversal query of k_trace_wave, from one ncu capture of the
-# same scene at 480x270, 4 spp (bounce-0 launch: 518,400 rays, 87.5 MB read + 8.2 MB
+# same scene at 480x270, 4 spp (bounce-0 launch: 518,400 rays, 77.4 MB read + 7.0 MB
 # written); the roofline scales it to a full launch by the launch's rays
-TRACE_DRAM_BYTES_PER_RAY = 184.7
+TRACE_DRAM_BYTES_PER_RAY = 162.8
 UNIT = "Mrays/s"
 WORKLOAD = "instanced 16 meshes / 1024 instances, 1920x1080, 64 spp, 8 bounces, equirect sky"
 
