@@ -122,6 +122,8 @@ typedef struct nb_scene_info {
   uint64_t n_vertices, n_triangles, n_instances, n_blas_roots;
   uint64_t n_blas_nodes_ref, n_tlas_nodes_ref;   /* reference-layout node counts */
   uint64_t n_blas_nodes_gpu, n_tlas_nodes_gpu;   /* device 8-wide node records */
+  uint64_t n_tlas_entries;                       /* device TLAS leaves: one per instance, one per
+                                                    BLAS-root child of a large instance */
   uint64_t device_bytes;
   double build_ms;                               /* host BVH build time */
 } nb_scene_info;

@@ -55,7 +55,8 @@ class NbEnvDesc(C.Structure):
 class NbSceneInfo(C.Structure):
     _fields_ = [("n_vertices", C.c_uint64), ("n_triangles", C.c_uint64), ("n_instances", C.c_uint64),
                 ("n_blas_roots", C.c_uint64), ("n_blas_nodes_ref", C.c_uint64), ("n_tlas_nodes_ref", C.c_uint64),
-                ("n_blas_nodes_gpu", C.c_uint64), ("n_tlas_nodes_gpu", C.c_uint64), ("device_bytes", C.c_uint64),
+                ("n_blas_nodes_gpu", C.c_uint64), ("n_tlas_nodes_gpu", C.c_uint64), ("n_tlas_entries", C.c_uint64),
+                ("device_bytes", C.c_uint64),
                 ("build_ms", C.c_double)]
 
 

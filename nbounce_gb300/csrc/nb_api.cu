@@ -268,6 +268,7 @@ int nb_scene_get_info(const nb_scene* s, nb_scene_info* info) {
   info->n_tlas_nodes_ref = h.tlas.size();
   info->n_blas_nodes_gpu = s->uploaded ? h.wblas_nodes : h.wblas.size();
   info->n_tlas_nodes_gpu = s->uploaded ? h.wtlas_nodes : h.wtlas.size();
+  info->n_tlas_entries = h.tlas_entries;
   info->device_bytes = s->arena.bytes;
   info->build_ms = h.build_ms;
   return NB_OK;

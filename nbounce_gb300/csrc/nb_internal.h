@@ -85,6 +85,7 @@ struct HostScene {
   std::vector<WideNode> wblas, wtlas;  // 8-wide trees; the TLAS root is wtlas[0]
   std::vector<uint32_t> wblas_root;    // per distinct BLAS root: index of its root in wblas
   size_t wblas_nodes = 0, wtlas_nodes = 0;  // sizes kept after the host copies are dropped
+  size_t tlas_entries = 0;                  // device TLAS leaves (itrace records)
   bool has_tlas = false;
   std::vector<GpuInstTrace> itrace;
   std::vector<GpuInstShade> ishade;

@@ -958,6 +958,7 @@ int to_device_layout(HostScene* s) {
   // boxes, collapsed like the BLAS; entries re-ordered by the wide TLAS
   s->wtlas.clear();
   s->itrace.clear();
+  s->tlas_entries = 0;
   s->ishade.assign(n_inst, GpuInstShade{});
   s->has_tlas = !s->tlas.empty() && n_inst > 0;
   if (s->has_tlas) {
@@ -975,6 +976,7 @@ int to_device_layout(HostScene* s) {
     Collapser ct{tlas, ebox, &s->wtlas, &order, 1};
     ct.build(0);  // raytracing_sw.wgsl:183-186: the TLAS root is node 0
     s->itrace.assign(order.size(), GpuInstTrace{});
+    s->tlas_entries = order.size();
     for (size_t k = 0; k < order.size(); ++k) {
       const TlasEntry& en = entries[eb[order[k]].payload];
       const nb_instance& in = s->instances[en.inst];

@@ -160,3 +160,31 @@ def test_non_finite_rays_hit_nothing(soup):
     good = ~bad
     assert np.sum(rf[good, 0] != NO_HIT) > 25  # 51 of the 256 finite rays meet the soup
     compare_hits(hits[good], inst[good], gpu.export()["indices"], rf[good], ru[good])
+
+
+def test_large_instance_split_into_tlas_entries_traces_like_the_oracle():
+    """The terrain of the instanced scene covers most of the scene, so the device TLAS enters
+    it once per child of its BLAS root (partial re-braiding) with tight world boxes; rays
+    grazing it and rays from above must find the oracle's closest hits (the oracle traverses
+    the reference TLAS over the transformed root boxes)."""
+    desc = scenes.instanced_scene(scale=1 / 64, n_instances=96, width=64, height=64, env_size=(16, 8))
+    gpu = nb.SceneBuffers.from_desc(desc)
+    orc = O.OracleScene(desc.vertices, desc.indices, desc.primitives(), dedup=True)
+    rng = np.random.default_rng(8)
+    n = 20000
+    rays = np.zeros((n, 8), np.float32)
+    half = n // 2
+    # from above, toward the terrain and the instances
+    rays[:half, :3] = rng.uniform([-40, 20, -40], [40, 30, 40], (half, 3))
+    d = rng.normal(size=(half, 3)) * [0.4, 1.0, 0.4]
+    d[:, 1] = -np.abs(d[:, 1])
+    rays[:half, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
+    # grazing: just above the terrain's level, nearly horizontal
+    rays[half:, :3] = rng.uniform([-40, -11.5, -40], [40, -8.0, 40], (n - half, 3))
+    g = rng.normal(size=(n - half, 3)) * [1.0, 0.05, 1.0]
+    rays[half:, 4:7] = g / np.linalg.norm(g, axis=1, keepdims=True)
+    hits, inst = gpu.trace_host(rays)
+    rf, ru, _ = orc.trace(rays)
+    assert gpu.info()["n_tlas_entries"] > len(desc.instances)  # the terrain was split
+    ties, both = compare_hits(hits, inst, gpu.export()["indices"], rf, ru)
+    assert both > n // 4

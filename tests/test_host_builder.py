@@ -144,3 +144,15 @@ def test_sobol_table_product_equals_oracle():
 def test_output_size_rule():
     assert nb.Pathtracer.output_size(1920, 1080, 0.3) == (576, 320)
     assert nb.Pathtracer.output_size(1920, 1080, 1.0) == (1920, 1080)
+
+
+def test_device_tlas_splits_only_large_instances():
+    """Device TLAS entries (host-only build): every instance enters once, except instances whose
+    box exceeds 2% of the scene's box area and whose BLAS root has only inner children - the
+    instanced scene's 45x terrain - which enter once per child of that root."""
+    spheres = scenes.spheres_scene(width=16, height=16)
+    s = nb.SceneBuffers.from_desc(spheres, host_only=True).info()
+    assert s["n_tlas_entries"] == s["n_instances"]
+    desc = scenes.instanced_scene(scale=1 / 64, n_instances=96, width=16, height=16, env_size=(16, 8))
+    i = nb.SceneBuffers.from_desc(desc, host_only=True).info()
+    assert i["n_instances"] < i["n_tlas_entries"] <= i["n_instances"] + 7 * 4
