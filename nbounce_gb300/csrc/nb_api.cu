@@ -728,7 +728,7 @@ int nb_pathtracer_output(const nb_pathtracer* pt, float** device_rgba, uint32_t*
 }
 
 int nb_pathtracer_download(const nb_pathtracer* pt, float* host_rgba, void* stream) {
-  if (!pt || (!host_rgba && pt->width * pt->height)) return fail(NB_ERR_INVALID_ARG, "NULL argument");
+  if (!pt || (!host_rgba && pt->width != 0 && pt->height != 0)) return fail(NB_ERR_INVALID_ARG, "NULL argument");
   size_t n = (size_t)pt->width * pt->height * 4 * sizeof(float);
   if (!n) return NB_OK;
   cudaStream_t st = (cudaStream_t)stream;

@@ -6,10 +6,11 @@
 //               jitter and generate_ray (pathtracing.wgsl:27-41, 245-255), queued in 8x8
 //               pixel tiles
 //   trace       persistent warps take 32 rays at a time with one atomic and walk 8-wide
-//               quantised trees collapsed from the reference's TLAS/BLAS (raytracing_sw.wgsl:
-//               176-319): one 80-byte node load tests eight child boxes, leaf triangles are
-//               tested as soon as their box is hit, and hit children are pushed in distance
-//               order so the nearest is visited next
+//               quantised trees (raytracing_sw.wgsl:176-319): BLASes collapsed from the
+//               reference's, a TLAS over tight world boxes of the instances (large instances
+//               split at their BLAS root).  One 80-byte node load tests eight child boxes; hit
+//               children are pushed in distance order so the nearest is visited next, then the
+//               node's hit leaf triangles are tested
 //   shade       hit attributes (raytracing_sw.wgsl:138-173), env/emission termination, lobe
 //               choice, VNDF / cosine sampling, Russian roulette (pathtracing.wgsl:161-241);
 //               each block appends its survivors to the next bounce's queue grouped by
@@ -19,9 +20,10 @@
 // of several jobs (render requests): tables of segments, jobs and scenes ride in the kernel
 // parameters and each path finds its job through its path id.
 //
-// The traversal finds the reference's closest hit: quantised boxes contain the reference
-// boxes, triangles are tested with the reference's Moller-Trumbore arithmetic, and a hit
-// replaces the current one only when strictly closer.  Visiting order differs from the
+// The traversal finds the reference's closest hit: quantised BLAS boxes contain the reference
+// boxes, TLAS boxes contain each instance's geometry, triangles are tested with the
+// reference's Moller-Trumbore arithmetic, and a hit replaces the current one only when
+// strictly closer.  Visiting order differs from the
 // reference (8-wide nodes, BLAS nodes pruned by the running closest hit where the reference
 // restarts each BLAS from NO_HIT, raytracing_sw.wgsl:255), so among triangles at exactly the
 // same distance another one may win: the documented near-tie class.

@@ -629,8 +629,8 @@ struct Collapser {
   struct DpNode {
     Item it;
     int32_t l = -1, r = -1;
-    float cost[8];     // C(x, i + 1)
-    uint8_t split[8];  // best slots for the left child when covering with i + 1 slots
+    float cost[8] = {};     // C(x, i + 1)
+    uint8_t split[8] = {};  // best slots for the left child when covering with i + 1 slots
     uint8_t fewer = 0; // bit i: C(x, i + 1) = C(x, i)
   };
   std::vector<DpNode> dp;
