@@ -206,3 +206,32 @@ def test_benchmark_scene_full_frame_crop_matches_oracle():
     crop = img[y0:y0 + h, x0:x0 + w]
     assert np.mean(np.all(crop == ref, axis=-1)) >= EXACT_FRAC
     assert rel_mse(crop, ref) <= REL_MSE
+
+
+def test_sample_shards_merged_equal_one_render():
+    """Sample sharding as the multi-GPU mode runs it (replicas.shard_samples /
+    merge_running_means): three Pathtracers each render a contiguous range of Sobol rows,
+    starting from sample counter start - 1; the merged running means equal one render of all
+    rows up to float rounding."""
+    from nbounce_gb300 import replicas
+    desc = scenes.spheres_scene(width=48, height=40, spp=10, bounces=6)
+    scene = nb.SceneBuffers.from_desc(desc)
+    env = nb.EnvMap(desc.env_color)
+    cam = nb.camera_struct(desc.world_to_clip, desc.clip_to_world)
+    full = nb.Pathtracer(desc.width, desc.height, nb.Globals(bounces=desc.bounces))
+    full.render(scene, cam, env, desc.spp)
+    ref = full.download()
+    means, lasts, counts = [], [], []
+    for r in range(3):
+        start, count = replicas.shard_samples(desc.spp, r, 3)
+        pt = nb.Pathtracer(desc.width, desc.height, nb.Globals(bounces=desc.bounces))
+        g = pt.globals
+        g.sample = start - 1
+        pt.globals = g
+        pt.render(scene, cam, env, count)
+        assert pt.last_stats()[1] == 0
+        means.append(pt.download())
+        lasts.append(start + count - 1)
+        counts.append(count)
+    merged = replicas.merge_running_means(means, lasts, counts)
+    np.testing.assert_allclose(merged, ref, rtol=2e-5, atol=2e-6)
