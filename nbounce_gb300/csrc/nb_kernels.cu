@@ -14,7 +14,7 @@
 //   shade       hit attributes (raytracing_sw.wgsl:138-173), env/emission termination, lobe
 //               choice, VNDF / cosine sampling, Russian roulette (pathtracing.wgsl:161-241);
 //               each block appends its survivors to the next bounce's queue grouped by
-//               direction octant (one atomic per block)
+//               direction bin (one atomic per block)
 //   accumulate  running mean over the batch's samples in sample order (pathtracing.wgsl:258)
 // so traversal runs in a lean kernel and the path state lives in HBM.  A wave can hold paths
 // of several jobs (render requests): tables of segments, jobs and scenes ride in the kernel
@@ -433,7 +433,7 @@ __global__ void __launch_bounds__(256) k_raygen(PathBatch pb, const WaveTables w
 // kSingle: every ray of the wave uses wt.scenes[0]; else the scene index carried in q_d.w.
 // Persistent warps take 32 consecutive rays per atomic and trace them together: consecutive
 // queue entries come from an 8x4 pixel patch (camera rays) or from one small patch of the
-// image with one direction octant (later bounces), so the lanes of a warp walk largely the
+// image with one direction bin (later bounces), so the lanes of a warp walk largely the
 // same nodes (shared cache lines, agreeing branches).  Refilling finished lanes one by one with
 // unrelated rays, with or without a warp-wide sync per node step, measured 11-30% slower.
 template <bool kSingle>
@@ -657,50 +657,59 @@ __device__ __forceinline__ float lambda_tr(float ndotv, float alpha2) {  // path
   return (-1.0f + sqrtf(1.0f + alpha2 * tan2)) / 2.0f;
 }
 
-// Appends the surviving rays of one block to the next bounce's queue grouped by
-// the octant of their direction (a counting sort over the block: one atomic per block).  The
-// block's input rays are neighbours in the image (tiled queue order), so each run of ~32
-// same-octant rays that a trace warp takes together starts from one small patch of the image
-// and points the same way; measured 12% faster secondary traversal than the input order.
-// The queue order changes no result: rays carry their path id.  Call from every thread of the
-// block (block-uniform control flow), alternating between two kSlots-word halves of sh from
-// one call to the next (the second barrier of a call then also protects the other half).
-template <int kThreads>
-struct AppendShape {
-  static constexpr int kWarps = kThreads / 32;
-  static constexpr int kSlots = kWarps * 8;      // (warp, octant) counts of one call
-  static constexpr int kPerLane = kSlots / 32;   // counts each lane of the scanning warp owns
-  static_assert(kThreads % 32 == 0 && kSlots % 32 == 0, "whole warps of 32 threads, 8 octants");
-};
+// Appends the surviving rays of one block to the next bounce's queue grouped by direction (a
+// counting sort over the block: one global atomic per block).  The block's input rays are
+// neighbours in the image (tiled queue order), so each run of same-bin rays that a trace warp
+// takes together starts from one small patch of the image and points nearly the same way.
+// Bins: the cube face of the direction's major axis (6) x a 4 x 4 grid of the other two
+// components over that face (96).  Against grouping by octant (itself 12% faster secondary
+// traversal than the input order): 6.5% faster on uniform-hemisphere probe rays, +0.6% on the
+// benchmark frame, whose cosine and GGX bounces the octant already groups well.
+// The queue order changes no result: rays carry their path id.  Call from every thread of
+// the block (block-uniform control flow); sh holds 2 kDirBins words, the first kDirBins
+// zero before the first call (append_init) - each call leaves them zero again.
+constexpr uint32_t kDirBins = 96;
+__device__ __forceinline__ uint32_t dir_bin(float4 d) {
+  const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+  float a, u, v;
+  uint32_t face;
+  if (ax >= ay && ax >= az) {
+    a = ax; face = d.x < 0.0f ? 1u : 0u; u = d.y; v = d.z;
+  } else if (ay >= az) {
+    a = ay; face = d.y < 0.0f ? 3u : 2u; u = d.z; v = d.x;
+  } else {  // also NaN directions: face 4, cell 0
+    a = az; face = d.z < 0.0f ? 5u : 4u; u = d.x; v = d.y;
+  }
+  const float h = 0.5f * a;
+  const uint32_t qu = (uint32_t)(u > -h) + (uint32_t)(u > 0.0f) + (uint32_t)(u > h);
+  const uint32_t qv = (uint32_t)(v > -h) + (uint32_t)(v > 0.0f) + (uint32_t)(v > h);
+  return face * 16u + qu * 4u + qv;
+}
+__device__ __forceinline__ void append_init(uint32_t* sh) {
+  for (uint32_t i = threadIdx.x; i < kDirBins; i += blockDim.x) sh[i] = 0u;
+  __syncthreads();
+}
 // k_shade: 512 threads capped at 64 registers (2 blocks per SM) measured 1.3% faster than 256
 // threads at 68 registers (3 blocks); the NEE and cache shade kernels (78 registers) stay at
 // 256 threads, where that cap would spill
 constexpr int kShadeThreads = 512;
 constexpr int kShadeExtThreads = 256;
-template <int kThreads>
-__device__ __forceinline__ uint32_t block_append_octant(uint32_t* counter, bool active, float4 dir, uint32_t* sh) {
-  using A = AppendShape<kThreads>;
-  const uint32_t oct = ((dir.x < 0.0f) ? 4u : 0u) | ((dir.y < 0.0f) ? 2u : 0u) | ((dir.z < 0.0f) ? 1u : 0u);
+__device__ __forceinline__ uint32_t block_append_binned(uint32_t* counter, bool active, float4 dir, uint32_t* sh) {
+  uint32_t* cnt = sh;
+  uint32_t* off = sh + kDirBins;
+  const uint32_t key = active ? dir_bin(dir) : kDirBins;  // kDirBins: no bin
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  const uint32_t below = (1u << lane) - 1u;
-  uint32_t rank = 0;
-#pragma unroll
-  for (uint32_t o = 0; o < 8; ++o) {
-    const uint32_t m = __ballot_sync(0xFFFFFFFFu, active && oct == o);
-    if (lane == (int)o) sh[warp * 8 + o] = (uint32_t)__popc(m);
-    if (active && oct == o) rank = (uint32_t)__popc(m & below);
-  }
+  const uint32_t grp = __match_any_sync(0xFFFFFFFFu, key);
+  const int leader = __ffs(grp) - 1;
+  uint32_t woff = 0;
+  if (active && lane == leader) woff = atomicAdd(&cnt[key], (uint32_t)__popc(grp));
+  woff = __shfl_sync(0xFFFFFFFFu, woff, leader);
+  const uint32_t rank = (uint32_t)__popc(grp & ((1u << lane) - 1u));
   __syncthreads();
-  if (warp == 0) {
-    // exclusive offsets in (octant, warp) order, i.e. runs of one octant; lane l owns the
-    // entries e = l * kPerLane + j, stored at sh[(e % kWarps) * 8 + e / kWarps]
-    uint32_t c[A::kPerLane], own = 0;
-#pragma unroll
-    for (int j = 0; j < A::kPerLane; ++j) {
-      const int e = lane * A::kPerLane + j;
-      c[j] = sh[(e % A::kWarps) * 8 + e / A::kWarps];
-      own += c[j];
-    }
+  if (warp == 0) {  // exclusive bin offsets, one global atomic; counts cleared for the next call
+    static_assert(kDirBins == 96, "three bins per lane of the scanning warp");
+    const uint32_t c0 = cnt[3 * lane], c1 = cnt[3 * lane + 1], c2 = cnt[3 * lane + 2];
+    const uint32_t own = c0 + c1 + c2;
     uint32_t incl = own;
 #pragma unroll
     for (int d = 1; d < 32; d <<= 1) {
@@ -711,15 +720,13 @@ __device__ __forceinline__ uint32_t block_append_octant(uint32_t* counter, bool 
     uint32_t base = 0;
     if (lane == 0 && total) base = atomicAdd(counter, total);
     base = __shfl_sync(0xFFFFFFFFu, base, 0) + incl - own;
-#pragma unroll
-    for (int j = 0; j < A::kPerLane; ++j) {
-      const int e = lane * A::kPerLane + j;
-      sh[(e % A::kWarps) * 8 + e / A::kWarps] = base;
-      base += c[j];
-    }
+    off[3 * lane] = base;
+    off[3 * lane + 1] = base + c0;
+    off[3 * lane + 2] = base + c0 + c1;
+    cnt[3 * lane] = cnt[3 * lane + 1] = cnt[3 * lane + 2] = 0u;
   }
   __syncthreads();
-  return sh[warp * 8 + oct] + rank;
+  return active ? off[key] + woff + rank : 0u;
 }
 
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool active) {
@@ -862,8 +869,9 @@ __device__ __forceinline__ float rr_continue(uint32_t bounce, const JobParams& j
 
 __global__ void __launch_bounds__(kShadeThreads, 2) k_shade(PathBatch pb, const WaveTables wt, uint32_t bounce) {
   __shared__ Segment segs[nb::kMaxWaveSegments];
-  __shared__ uint32_t append_sh[2 * AppendShape<kShadeThreads>::kSlots];
+  __shared__ uint32_t append_sh[2 * kDirBins];
   stage_segments(segs, wt);
+  append_init(append_sh);
   const uint32_t n = pb.counts[bounce];
   const bool odd = (bounce & 1) != 0;
   const float4* __restrict__ in_o = odd ? pb.q_o[1] : pb.q_o[0];
@@ -873,7 +881,7 @@ __global__ void __launch_bounds__(kShadeThreads, 2) k_shade(PathBatch pb, const 
   float4* __restrict__ out_d = odd ? pb.q_d[0] : pb.q_d[1];
   float4* __restrict__ out_t = odd ? pb.q_t[0] : pb.q_t[1];
   const uint32_t stride = gridDim.x * blockDim.x;
-  // whole blocks iterate together: block_append_octant synchronises the block
+  // whole blocks iterate together: block_append_binned synchronises the block
   for (uint32_t base = blockIdx.x * blockDim.x; base < n; base += stride) {
     const uint32_t i = base + threadIdx.x;
     bool cont = false;
@@ -914,8 +922,7 @@ __global__ void __launch_bounds__(kShadeThreads, 2) k_shade(PathBatch pb, const 
         }
       }
     }
-    const uint32_t slot = block_append_octant<kShadeThreads>(
-        pb.counts + bounce + 1, cont, next_d, append_sh + ((base / stride) & 1u) * AppendShape<kShadeThreads>::kSlots);
+    const uint32_t slot = block_append_binned(pb.counts + bounce + 1, cont, next_d, append_sh);
     if (cont) {
       out_o[slot] = next_o;
       out_d[slot] = next_d;
@@ -962,8 +969,9 @@ __global__ void __launch_bounds__(kShadeExtThreads) k_shade_cache(PathBatch pb, 
                                                      uint32_t bounce) {
   using nb::CacheQuery;
   __shared__ Segment segs[nb::kMaxWaveSegments];
-  __shared__ uint32_t append_sh[2 * AppendShape<kShadeExtThreads>::kSlots];
+  __shared__ uint32_t append_sh[2 * kDirBins];
   stage_segments(segs, wt);
+  append_init(append_sh);
   const uint32_t n = pb.counts[bounce];
   const bool odd = (bounce & 1) != 0;
   const float4* __restrict__ in_o = odd ? pb.q_o[1] : pb.q_o[0];
@@ -1083,8 +1091,7 @@ __global__ void __launch_bounds__(kShadeExtThreads) k_shade_cache(PathBatch pb, 
         }
       }
     }
-    const uint32_t at = block_append_octant<kShadeExtThreads>(
-        pb.counts + bounce + 1, cont, next_d, append_sh + ((base / stride) & 1u) * AppendShape<kShadeExtThreads>::kSlots);
+    const uint32_t at = block_append_binned(pb.counts + bounce + 1, cont, next_d, append_sh);
     if (cont) {
       out_o[at] = next_o;
       out_d[at] = next_d;
@@ -1170,8 +1177,9 @@ __device__ __forceinline__ bool finite3(V3 v) { return isfinite(v.x) && isfinite
 __global__ void __launch_bounds__(kShadeExtThreads) k_shade_nee(PathBatch pb, const WaveTables wt, const ShadowQueue sq,
                                                    uint32_t bounce) {
   __shared__ Segment segs[nb::kMaxWaveSegments];
-  __shared__ uint32_t append_sh[2 * AppendShape<kShadeExtThreads>::kSlots];
+  __shared__ uint32_t append_sh[2 * kDirBins];
   stage_segments(segs, wt);
+  append_init(append_sh);
   const uint32_t n = pb.counts[bounce];
   const bool odd = (bounce & 1) != 0;
   const float4* __restrict__ in_o = odd ? pb.q_o[1] : pb.q_o[0];
@@ -1254,8 +1262,7 @@ __global__ void __launch_bounds__(kShadeExtThreads) k_shade_nee(PathBatch pb, co
         }
       }
     }
-    const uint32_t slot = block_append_octant<kShadeExtThreads>(
-        pb.counts + bounce + 1, cont, next_d, append_sh + ((base / stride) & 1u) * AppendShape<kShadeExtThreads>::kSlots);
+    const uint32_t slot = block_append_binned(pb.counts + bounce + 1, cont, next_d, append_sh);
     if (cont) {
       out_o[slot] = next_o;
       out_d[slot] = next_d;
