@@ -244,3 +244,35 @@ def test_concurrent_submitters_get_their_own_images(world):
         assert np.array_equal(out, alone(world, *job, env_nee=nee)), job
     assert srv.stats()["jobs_done"] == 12
     srv.close()
+
+
+def test_burst_of_small_jobs_completes_and_frees_its_memory(world):
+    """Four hundred small jobs submitted at once (sizes, sample counts and estimators mixed):
+    every job completes, admission never exceeds the budget, and once the images are delivered
+    and the jobs released the server holds only its fixed buffers again."""
+    paths = 1 << 15
+    budget = fixed_bytes(paths) + 64 * 64 * 16 * 24  # room for ~24 of the largest images at once
+    srv = RenderServer(hbm_budget_bytes=budget, paths_per_wave=paths)
+    slots = [srv.add_scene(s) for s in world["scenes"]]
+    env_slots = [srv.add_env(e) for e in world["envs"]]
+    rng = np.random.default_rng(17)
+    idle = srv.stats()["bytes_in_use"]
+    jobs = []
+    for n in range(400):
+        k = int(rng.integers(2))
+        w, h = int(rng.integers(8, 65)), int(rng.integers(8, 65))
+        spp, b = int(rng.integers(1, 5)), int(rng.integers(0, 9))
+        flags = [0, L.NB_JOB_ENV_NEE, L.NB_JOB_CACHE][int(rng.integers(3))]
+        w2c, c2w = scenes.camera_matrices(*CAMS[k], w, h)
+        jobs.append((srv.submit(slots[k], env_slots[k], w2c, c2w, w, h, spp, b, flags=flags), w, h))
+    for jid, w, h in jobs:
+        info = srv.wait(jid, timeout_ms=300000)
+        assert info["done"] == 1 and info["status"] == 0
+        img = srv.fetch(jid, w, h)
+        assert np.isfinite(img).all() and (img[..., 3] == 1.0).all()
+        srv.release(jid)
+    st = srv.stats()
+    assert st["jobs_done"] == 400 and st["jobs_failed"] == 0
+    assert st["peak_bytes_in_use"] <= budget
+    assert st["bytes_in_use"] == idle
+    srv.close()
