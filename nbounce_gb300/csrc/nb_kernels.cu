@@ -751,6 +751,11 @@ struct HitSurface {
 
 __device__ __forceinline__ void load_hit_surface(const DevScene& s, uint32_t inst, float4 O, float4 H, V3 rdir,
                                                  HitSurface& hs) {
+  // the triangle's vertex indices are loaded before the instance record is looked at, so the
+  // two loads overlap (they are valid for every hit, emissive or not)
+  const uint32_t tri = __float_as_uint(H.w);
+  const uint32_t i0 = __ldg(s.tri_idx + 3 * (size_t)tri), i1 = __ldg(s.tri_idx + 3 * (size_t)tri + 1),
+                 i2 = __ldg(s.tri_idx + 3 * (size_t)tri + 2);
   const float4* sh = s.inst_shade + 6 * (size_t)inst;
   const float4 c0 = ld4(sh), c1 = ld4(sh + 1), c2 = ld4(sh + 2);
   const float4 l0 = ld4(sh + 3), l1 = ld4(sh + 4), l2 = ld4(sh + 5);
@@ -760,9 +765,6 @@ __device__ __forceinline__ void load_hit_surface(const DevScene& s, uint32_t ins
   hs.emissive = l2.w > 0.0f;  // EMISSIVE (raytracing_sw.wgsl:168-170)
   if (hs.emissive) return;
   // hit attributes (raytracing_sw.wgsl:146-158)
-  const uint32_t tri = __float_as_uint(H.w);
-  const uint32_t i0 = __ldg(s.tri_idx + 3 * (size_t)tri), i1 = __ldg(s.tri_idx + 3 * (size_t)tri + 1),
-                 i2 = __ldg(s.tri_idx + 3 * (size_t)tri + 2);
   const float4 a0 = ld4(s.vattr + 2 * (size_t)i0), a1 = ld4(s.vattr + 2 * (size_t)i1),
                a2 = ld4(s.vattr + 2 * (size_t)i2);
   const float4 b0 = ld4(s.vattr + 2 * (size_t)i0 + 1), b1 = ld4(s.vattr + 2 * (size_t)i1 + 1),
