@@ -102,7 +102,8 @@ typedef struct nb_camera {
 } nb_camera;
 
 /* Environment seen by rays that miss (pathtracing.wgsl:167-170).  The reference samples a
- * BC6H cube map; this ABI takes a constant colour or an equirect RGBA32F map. */
+ * BC6H cube map: nb_env_create_dds takes that file; this descriptor takes a constant colour,
+ * an equirect RGBA32F map or six RGBA32F cube faces. */
 enum { NB_ENV_CONSTANT = 0, NB_ENV_EQUIRECT = 1, NB_ENV_CUBE = 2 };
 typedef struct nb_env_desc {
   uint32_t kind;
@@ -191,6 +192,19 @@ void nb_scene_destroy(nb_scene* scene);
  * ------------------------------------------------------------------------------------- */
 int nb_env_create(const nb_env_desc* desc, nb_env** out);
 void nb_env_destroy(nb_env* env);
+/* EnvMap::load / Texture::create_cubemap (envmap.rs:12-17, texture.rs:89-144): an environment
+ * from the bytes of a DDS cube-map file.  DXGI BC6H_UF16 - the reference's only format - and
+ * BC6H_SF16 are decoded on the device; R16G16B16A16_FLOAT and R32G32B32A32_FLOAT (DX10 header,
+ * or the legacy FourCC codes 113 / 116 with the cube-map caps bit) are read as they are.  A DX10
+ * file is read as six array layers (+X, -X, +Y, -Y, +Z, -Z) whatever its array size says, as
+ * texture.rs:95-96 forces them; of each layer's mip chain only level 0 is kept, the level the
+ * pass samples (pathtracing.wgsl:168).  The result is an NB_ENV_CUBE environment. */
+int nb_env_create_dds(const void* bytes, size_t n, nb_env** out);
+/* BC6H block decoding on the device, host buffers in and out: blocks holds layers x
+ * ceil(height / 4) x ceil(width / 4) 16-byte blocks in row-major block order; out receives
+ * layers x height x width RGBA32F texels (alpha 1).  is_signed: 0 = BC6H_UF16, 1 = BC6H_SF16. */
+int nb_bc6h_decode(const void* blocks, uint32_t width, uint32_t height, uint32_t layers, uint32_t is_signed,
+                   float* out);
 
 /* ---------------------------------------------------------------------------------------
  * The pass (Pathtracer, src/pathtracing/pathtracer.rs:15-239)

@@ -139,6 +139,8 @@ def lib():
         "nb_scene_destroy": ([vp], None),
         "nb_env_create": ([vp, vp], i32),
         "nb_env_destroy": ([vp], None),
+        "nb_env_create_dds": ([vp, sz, vp], i32),
+        "nb_bc6h_decode": ([vp, u32, u32, u32, u32, vp], i32),
         "nb_pathtracer_create": ([u32, u32, vp, vp, u32, vp], i32),
         "nb_pathtracer_destroy": ([vp], None),
         "nb_pathtracer_dispatch": ([vp, vp, vp, vp, vp], i32),

@@ -26,7 +26,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompil
               "-I", CSRC, "-I", INCLUDE]
 CXX_FLAGS = ["-O3", "-std=c++17", "-fPIC", "-pthread", "-ffp-contract=off", "-fno-fast-math", "-Wall",
              "-I", CSRC, "-I", INCLUDE]
-CU_SOURCES = ["nb_kernels.cu", "nb_api.cu", "nb_server.cu", "nb_static.cu", "nb_cache.cu"]
+CU_SOURCES = ["nb_kernels.cu", "nb_api.cu", "nb_server.cu", "nb_static.cu", "nb_cache.cu", "nb_bc6h.cu"]
 CXX_SOURCES = ["nb_scene.cpp", "nb_sobol.cpp"]
 HEADERS = ["nb_internal.h", "nb_device.cuh", "nb_launch.h", "nb_runtime.h", "nb_mlp.cuh", "sobol_directions.inc"]
 

@@ -16,6 +16,8 @@
 #include <tuple>
 #include <vector>
 
+#include <cuda_fp16.h>
+
 #include "nb_internal.h"
 #include "nb_mlp.cuh"
 #include "nb_launch.h"
@@ -287,9 +289,7 @@ void nb_scene_destroy(nb_scene* s) {
 // cube face - with negative or non-finite luminance counted as 0 and a uniform luminance if
 // the whole map is black.  Sums in double, tables in float: marginal CDF over rows, a CDF per
 // row, and per texel the density over the table's (u, v) = w / sum(w) x width x height.
-static int build_env_distribution(nb_env* e, const nb_env_desc* desc) {
-  const bool cube = desc->kind == NB_ENV_CUBE;
-  const uint32_t W = desc->width, H = cube ? 6 * desc->height : desc->height;
+static int build_env_distribution(nb_env* e, const float* texels, uint32_t W, uint32_t H, bool cube) {
   std::vector<double> w((size_t)W * H), row_sum(H, 0.0);
   double total = 0.0;
   for (int pass = 0; pass < 2 && !(total > 0.0); ++pass) {
@@ -299,7 +299,7 @@ static int build_env_distribution(nb_env* e, const nb_env_desc* desc) {
       const double tc = 2.0 * ((double)(y % W) + 0.5) / (double)W - 1.0;  // cube: t of the row
       double r = 0.0;
       for (uint32_t x = 0; x < W; ++x) {
-        const float* t = desc->texels + ((size_t)y * W + x) * 4;
+        const float* t = texels + ((size_t)y * W + x) * 4;
         double lum = pass == 0 ? 0.2126 * t[0] + 0.7152 * t[1] + 0.0722 * t[2] : 1.0;
         if (!(lum > 0.0) || !std::isfinite(lum)) lum = 0.0;
         double omega = sin_t;
@@ -371,13 +371,99 @@ int nb_env_create(const nb_env_desc* desc, nb_env** out) {
     e->dev.texels = (const float4*)p;
     e->dev.width = desc->width;
     e->dev.height = rows;
-    if ((st = build_env_distribution(e, desc))) {
+    if ((st = build_env_distribution(e, desc->texels, desc->width, rows, desc->kind == NB_ENV_CUBE))) {
       e->arena.release();
       delete e;
       return st;
     }
   }
   *out = e;
+  return NB_OK;
+}
+
+int nb_env_create_dds(const void* bytes, size_t n, nb_env** out) {
+  if (!bytes || !out) return fail(NB_ERR_INVALID_ARG, "NULL argument");
+  *out = nullptr;
+  DdsCube dds;
+  int st = parse_dds_cube((const uint8_t*)bytes, n, &dds);
+  if (st) return st;
+  if ((st = check_device())) return st;
+  const uint32_t N = dds.size;
+  const size_t n_texels = (size_t)6 * N * N;
+  std::vector<float> host(n_texels * 4);
+  nb_env* e = new (std::nothrow) nb_env();
+  if (!e) return fail(NB_ERR_OOM, "host allocation failed");
+  auto bail = [&](int status) {
+    e->arena.release();
+    delete e;
+    return status;
+  };
+  void* texels = nullptr;
+  if ((st = e->arena.alloc(n_texels * sizeof(float4), &texels))) return bail(st);
+  if (dds.format == kDdsBc6hUf16 || dds.format == kDdsBc6hSf16) {
+    DeviceArena blocks;
+    void* d_blocks = nullptr;
+    if ((st = blocks.alloc(6 * dds.face_bytes, &d_blocks))) return bail(st);
+    cudaError_t ce = cudaSuccess;
+    for (int f = 0; f < 6 && ce == cudaSuccess; ++f)
+      ce = cudaMemcpy((uint8_t*)d_blocks + f * dds.face_bytes, dds.face[f], dds.face_bytes, cudaMemcpyHostToDevice);
+    if (ce == cudaSuccess) {
+      st = decode_bc6h_device(d_blocks, N, N, 6, dds.format == kDdsBc6hSf16, (float4*)texels, 0);
+      if (!st) ce = cudaMemcpy(host.data(), texels, n_texels * sizeof(float4), cudaMemcpyDeviceToHost);
+    }
+    blocks.release();
+    if (st) return bail(st);
+    if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaMemcpy(env blocks)"));
+  } else {
+    const size_t face_texels = (size_t)N * N;
+    for (int f = 0; f < 6; ++f) {
+      float* dst = host.data() + f * face_texels * 4;
+      if (dds.format == kDdsRgba32f) {
+        std::memcpy(dst, dds.face[f], face_texels * 16);
+      } else {
+        for (size_t i = 0; i < face_texels * 4; ++i) {
+          __half_raw raw;
+          std::memcpy(&raw.x, dds.face[f] + 2 * i, 2);
+          dst[i] = __half2float(__half(raw));
+        }
+      }
+    }
+    cudaError_t ce = cudaMemcpy(texels, host.data(), n_texels * sizeof(float4), cudaMemcpyHostToDevice);
+    if (ce != cudaSuccess) return bail(cuda_fail(ce, "cudaMemcpy(env)"));
+  }
+  e->dev.kind = NB_ENV_CUBE;
+  e->dev.texels = (const float4*)texels;
+  e->dev.width = N;
+  e->dev.height = 6 * N;
+  if ((st = build_env_distribution(e, host.data(), N, 6 * N, true))) return bail(st);
+  *out = e;
+  return NB_OK;
+}
+
+int nb_bc6h_decode(const void* blocks, uint32_t width, uint32_t height, uint32_t layers, uint32_t is_signed,
+                   float* out) {
+  if (is_signed > 1) return fail(NB_ERR_INVALID_ARG, "is_signed must be 0 or 1");
+  if (width == 0 || height == 0 || layers == 0) return NB_OK;
+  if (!blocks || !out) return fail(NB_ERR_INVALID_ARG, "NULL argument");
+  if (width > 65536 || height > 65536) return fail(NB_ERR_INVALID_ARG, "BC6H size %u x %u", width, height);
+  int st = check_device();
+  if (st) return st;
+  const size_t in_bytes = (size_t)((width + 3) / 4) * ((height + 3) / 4) * layers * 16;
+  const size_t out_bytes = (size_t)width * height * layers * sizeof(float4);
+  DeviceArena tmp;
+  void *d_in = nullptr, *d_out = nullptr;
+  if ((st = tmp.alloc(in_bytes, &d_in)) || (st = tmp.alloc(out_bytes, &d_out))) {
+    tmp.release();
+    return st;
+  }
+  cudaError_t ce = cudaMemcpy(d_in, blocks, in_bytes, cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) {
+    st = decode_bc6h_device(d_in, width, height, layers, is_signed != 0, (float4*)d_out, 0);
+    if (!st) ce = cudaMemcpy(out, d_out, out_bytes, cudaMemcpyDeviceToHost);
+  }
+  tmp.release();
+  if (st) return st;
+  if (ce != cudaSuccess) return cuda_fail(ce, "cudaMemcpy(bc6h)");
   return NB_OK;
 }
 

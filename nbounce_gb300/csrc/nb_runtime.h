@@ -62,6 +62,21 @@ struct DeviceArena {
   }
 };
 
+// nb_bc6h.cu: BC6H blocks (layers x ceil(height / 4) x ceil(width / 4) 16-byte blocks, device)
+// decoded into layers x height x width RGBA32F texels (device), alpha 1.
+int decode_bc6h_device(const void* d_blocks, uint32_t width, uint32_t height, uint32_t layers, bool is_signed,
+                       float4* d_out, cudaStream_t stream);
+
+// nb_bc6h.cu: a DDS cube map's format, face size and the mip-0 data of its six faces.
+enum DdsFormat : uint32_t { kDdsBc6hUf16, kDdsBc6hSf16, kDdsRgba16f, kDdsRgba32f };
+struct DdsCube {
+  uint32_t format = 0;
+  uint32_t size = 0;
+  const uint8_t* face[6] = {};
+  size_t face_bytes = 0;
+};
+int parse_dds_cube(const uint8_t* bytes, size_t n, DdsCube* out);
+
 }  // namespace nb
 
 struct nb_scene {

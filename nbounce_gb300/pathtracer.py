@@ -148,8 +148,8 @@ class SceneBuffers:
 
 class EnvMap:
     """Constant colour, equirect RGBA32F (texels: (h, w, 4)) or cube-map RGBA32F (cube:
-    (6, n, n, 4), faces +X, -X, +Y, -Y, +Z, -Z) environment on the device (EnvMap::load,
-    envmap.rs:12)."""
+    (6, n, n, 4), faces +X, -X, +Y, -Y, +Z, -Z) environment on the device; ``from_dds`` loads
+    a DDS cube-map file as EnvMap::load does (envmap.rs:12)."""
 
     def __init__(self, color=(0.5, 0.6, 0.8), texels=None, cube=None):
         d = L.NbEnvDesc()
@@ -173,6 +173,25 @@ class EnvMap:
         check(lib().nb_env_create(C.byref(d), C.byref(h)))
         self._h = h
         self._tex = None
+
+    @classmethod
+    def from_dds(cls, source):
+        """EnvMap::load (envmap.rs:12-17): the cube map in a DDS file (a path or its bytes).
+        BC6H_UF16 - the reference's format - and BC6H_SF16 are decoded on the device; RGBA16F
+        and RGBA32F cube files are read as they are.  Mip 0 of each face is kept."""
+        if isinstance(source, (bytes, bytearray, memoryview)):
+            data = bytes(source)
+        else:
+            with open(source, "rb") as f:
+                data = f.read()
+        buf = C.create_string_buffer(data, len(data))
+        env = cls.__new__(cls)
+        env._tex = None
+        env._h = None
+        h = C.c_void_p()
+        check(lib().nb_env_create_dds(buf, len(data), C.byref(h)))
+        env._h = h
+        return env
 
     @property
     def handle(self):

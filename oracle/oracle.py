@@ -60,6 +60,8 @@ def lib():
                                 vp, vp, i32, i32, vp, vp, u32]
         L.or_render.restype = u64
         L.or_env_lookup.argtypes = [vp, vp, u64, i32, vp]
+        L.or_bc6h_decode_blocks.argtypes = [vp, C.c_size_t, i32, vp]
+        L.or_bc6h_decode.argtypes = [vp, u32, u32, u32, i32, vp]
         _lib = L
     return _lib
 
@@ -220,4 +222,23 @@ def primary_rays(clip_to_world, width, height, sobol, sample):
     sob = np.ascontiguousarray(sobol, dtype=np.float32)
     out = np.zeros((height * width, 8), np.float32)
     lib().or_primary_rays(_p(c2w), width, height, _p(sob), sob.size // 4, sample, _p(out))
+    return out
+
+
+def bc6h_decode_blocks(blocks, signed=False):
+    """Half-float bits (n, 16, 3) of n BC6H blocks ((n, 16) bytes): texels row-major in the
+    block, channels RGB (bc6h.cpp)."""
+    b = np.ascontiguousarray(blocks, dtype=np.uint8).reshape(-1, 16)
+    out = np.empty((b.shape[0], 16, 3), np.uint16)
+    lib().or_bc6h_decode_blocks(_p(b), C.c_size_t(b.shape[0]), C.c_int(1 if signed else 0), _p(out))
+    return out
+
+
+def bc6h_decode(blocks, width, height, layers=1, signed=False):
+    """(layers, height, width, 4) float32 texels (alpha 1) of BC6H blocks in row-major block
+    order, (layers, ceil(h/4), ceil(w/4), 16) bytes (bc6h.cpp)."""
+    b = np.ascontiguousarray(blocks, dtype=np.uint8)
+    out = np.empty((layers, height, width, 4), np.float32)
+    lib().or_bc6h_decode(_p(b), C.c_uint32(width), C.c_uint32(height), C.c_uint32(layers),
+                         C.c_int(1 if signed else 0), _p(out))
     return out
