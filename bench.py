@@ -40,9 +40,9 @@ if ROOT not in sys.path:
 
 METRIC = "Mrays/s (primary + extension rays), 1920x1080 64spp 8 bounces"
 # DRAM bytes (read + write) per traversal query of k_trace_wave, from one ncu capture of the
-# same scene at 480x270, 4 spp (bounce-0 launch: 518,400 rays, 77.4 MB read + 7.0 MB
+# same scene at 480x270, 4 spp (bounce-0 launch: 518,400 rays, 74.1 MB read + 6.0 MB
 # written); the roofline scales it to a full launch by the launch's rays
-TRACE_DRAM_BYTES_PER_RAY = 162.8
+TRACE_DRAM_BYTES_PER_RAY = 154.6
 UNIT = "Mrays/s"
 WORKLOAD = "instanced 16 meshes / 1024 instances, 1920x1080, 64 spp, 8 bounces, equirect sky"
 
@@ -573,7 +573,7 @@ def run_ours(args):
                             "note": "achieved counts the reference algorithm's bytes per query (binary BVH: 32 B "
                                     "per box test, 48 per triangle, 128 per instance, counted by the oracle); "
                                     "the device traversal fetches ~1.2-2.0 KB per ray (8-wide nodes, mostly "
-                                    "L1/L2 hits) and ~163 B from DRAM (traffic), hence frac > 1: the kernel is "
+                                    "L1/L2 hits) and ~155 B from DRAM (traffic), hence frac > 1: the kernel is "
                                     "latency-bound, not HBM-bound",
                             "kernel": "k_trace_wave", "peak_kind": f"{peak_kind} hbm_gbs (burst copy)",
                             "bytes_per_ray": round(bytes_per_ray, 1),
