@@ -50,6 +50,14 @@ def _level_bytes(dxgi, w, h):
     return w * h * (16 if dxgi == DXGI_R32G32B32A32_FLOAT else 8)
 
 
+def _block_bytes(blocks):
+    """The bytes of BC6H blocks given as bytes or as an array of any integer type (its memory
+    taken as it is, not converted element by element)."""
+    if isinstance(blocks, np.ndarray):
+        return np.ascontiguousarray(blocks).reshape(-1).view(np.uint8)
+    return np.frombuffer(bytes(blocks), np.uint8)
+
+
 def parse_cube_dds(data):
     """The format (a DXGI code), face size and mip-0 bytes of the six faces of a cube-map DDS
     file (bytes or a path), accepting what ``nb_env_create_dds`` accepts."""
@@ -100,8 +108,7 @@ def decode_bc6h(blocks, width, height, layers=1, signed=False):
     """BC6H blocks ((layers, ceil(h/4), ceil(w/4), 16) bytes, or the same bytes flat) decoded by
     the library on the device into (layers, height, width, 4) float32 (alpha 1)."""
     from . import _lib as L
-    src = np.ascontiguousarray(np.frombuffer(bytes(blocks), np.uint8) if not isinstance(blocks, np.ndarray)
-                               else blocks, dtype=np.uint8)
+    src = _block_bytes(blocks)
     need = ((width + 3) // 4) * ((height + 3) // 4) * layers * 16
     if src.size != need:
         raise ValueError(f"{src.size} bytes of BC6H blocks, {need} expected for {layers} x {width} x {height}")
@@ -162,7 +169,7 @@ def write_cube_dds_bc6h(blocks, n, signed=False, path=None, mip_blocks=None):
     ((6, ceil(n/4), ceil(n/4), 16) bytes).  mip_blocks, if given, lists per face the bytes of
     the further mip levels, written after each face's level 0.  Returns the bytes, also written
     to path if given."""
-    b = np.ascontiguousarray(blocks, dtype=np.uint8).reshape(6, -1)
+    b = _block_bytes(blocks).reshape(6, -1)
     per_face = ((n + 3) // 4) ** 2 * 16
     if b.shape[1] != per_face:
         raise ValueError(f"{b.shape[1]} bytes per face, {per_face} expected for n = {n}")

@@ -228,7 +228,7 @@ def primary_rays(clip_to_world, width, height, sobol, sample):
 def bc6h_decode_blocks(blocks, signed=False):
     """Half-float bits (n, 16, 3) of n BC6H blocks ((n, 16) bytes): texels row-major in the
     block, channels RGB (bc6h.cpp)."""
-    b = np.ascontiguousarray(blocks, dtype=np.uint8).reshape(-1, 16)
+    b = np.ascontiguousarray(blocks).reshape(-1).view(np.uint8).reshape(-1, 16)
     out = np.empty((b.shape[0], 16, 3), np.uint16)
     lib().or_bc6h_decode_blocks(_p(b), C.c_size_t(b.shape[0]), C.c_int(1 if signed else 0), _p(out))
     return out
@@ -237,7 +237,10 @@ def bc6h_decode_blocks(blocks, signed=False):
 def bc6h_decode(blocks, width, height, layers=1, signed=False):
     """(layers, height, width, 4) float32 texels (alpha 1) of BC6H blocks in row-major block
     order, (layers, ceil(h/4), ceil(w/4), 16) bytes (bc6h.cpp)."""
-    b = np.ascontiguousarray(blocks, dtype=np.uint8)
+    b = np.ascontiguousarray(blocks).reshape(-1).view(np.uint8)
+    need = ((width + 3) // 4) * ((height + 3) // 4) * layers * 16
+    if b.size != need:
+        raise ValueError(f"{b.size} bytes of BC6H blocks, {need} expected")
     out = np.empty((layers, height, width, 4), np.float32)
     lib().or_bc6h_decode(_p(b), C.c_uint32(width), C.c_uint32(height), C.c_uint32(layers),
                          C.c_int(1 if signed else 0), _p(out))

@@ -72,3 +72,13 @@ def test_oracle_matches_the_texture_unit(fmt):
     # BC6H has no alpha: CUDA's texture path fills it with 0 (the stored *_alpha), graphics
     # APIs with 1 as the decoders here do; the pass reads the environment's RGB only.
     assert np.all(g[fmt + "_alpha"] == 0.0)
+
+
+def test_block_arrays_of_any_integer_type_are_read_as_bytes():
+    blk = pack([(0b00011, 5), (512, 10), (0, 10), (0, 10), (0, 10), (0, 10), (0, 10), (0, 63)])
+    want = O.bc6h_decode_blocks(blk)
+    for dt in (np.uint16, np.uint32, np.uint64):
+        assert np.array_equal(O.bc6h_decode_blocks(blk.view(dt)), want)
+        assert np.array_equal(O.bc6h_decode(blk.view(dt), 4, 4), O.bc6h_decode(blk, 4, 4))
+    with pytest.raises(ValueError, match="expected"):
+        O.bc6h_decode(blk, 8, 4)

@@ -123,3 +123,11 @@ def test_sky_through_dds_keeps_the_cube():
     cube = scenes.cube_from_equirect(scenes.sky_envmap(2, 128, 64, sun_radiance=50.0), 16)
     got = dds.read_cube_dds(dds.write_cube_dds(cube, half=False))
     np.testing.assert_array_equal(got, cube)
+
+
+def test_bc6h_writer_takes_block_arrays_of_any_integer_type():
+    rng = np.random.default_rng(3)
+    blocks = rng.integers(0, 256, size=(6, 2, 2, 16), dtype=np.uint8)
+    want = dds.write_cube_dds_bc6h(blocks, 8)
+    assert dds.write_cube_dds_bc6h(blocks.view(np.uint32), 8) == want
+    assert dds.write_cube_dds_bc6h(blocks.view(np.uint64).reshape(6, -1), 8) == want
