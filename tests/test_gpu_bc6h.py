@@ -136,8 +136,9 @@ def test_dds_mip_chain_and_float_formats_give_the_same_environment():
 
 
 def test_dds_environment_importance_sampling_matches_its_texels():
-    """The NEE tables of a DDS environment are built from the decoded texels: sampled
-    directions carry the density env_pdf gives them, like a cube built from the same floats."""
+    """The NEE tables of a DDS environment are built from the decoded texels: the same uniform
+    numbers give bit-identical directions and densities as a cube built from the oracle's
+    decode of the same blocks."""
     rng = np.random.default_rng(13)
     n = 16
     blocks = smooth_cube_blocks(n, rng)
