@@ -526,14 +526,16 @@ struct Collapser {
   struct Span {
     uint32_t first = 0xFFFFFFFFu, end = 0, count = 0;
   };
-  mutable std::vector<Span> span;  // memo: primitive range and leaf count of a subtree
+  // memo: primitive range and leaf count of a subtree, one entry per binary node, sized by the
+  // caller; collapsers of disjoint trees share it (each writes only its own nodes' entries)
+  std::vector<Span>* span = nullptr;
 
   // [first, end) of the primitives below binary node n.  bvh.rs partitions in place, so a
   // subtree covers a contiguous range (count == end - first); trees handed in through
   // nb_scene_create_from_bvh are only trusted where that holds.
   Span subtree_span(uint32_t n) const {
-    if (span.empty()) span.assign(ref.size(), Span{});
-    if (span[n].first != 0xFFFFFFFFu) return span[n];
+    std::vector<Span>& memo = *span;
+    if (memo[n].first != 0xFFFFFFFFu) return memo[n];
     const nb_bvh_node& b = ref[n];
     Span r;
     if (b.end > 0) {
@@ -542,7 +544,7 @@ struct Collapser {
       Span l = subtree_span(b.start), h = subtree_span(b.start + 1);
       r = Span{std::min(l.first, h.first), std::max(l.end, h.end), l.count + h.count};
     }
-    span[n] = r;
+    memo[n] = r;
     return r;
   }
 
@@ -743,10 +745,30 @@ struct Collapser {
   }
 };
 
+// f(i) for i in [0, n) over up to 16 threads in chunks (f writes only its own elements)
+template <class F>
+void parallel_for(size_t n, F f) {
+  const size_t chunk = 1 << 16;
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const size_t n_chunks = (n + chunk - 1) / chunk;
+  if (hw == 1 || n_chunks < 2) {
+    for (size_t i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<size_t> next{0};
+  std::vector<std::thread> pool;
+  for (unsigned w = 0; w < std::min<size_t>(hw, n_chunks); ++w)
+    pool.emplace_back([&] {
+      for (size_t c; (c = next.fetch_add(1)) < n_chunks;)
+        for (size_t i = c * chunk, e = std::min(n, i + chunk); i < e; ++i) f(i);
+    });
+  for (std::thread& th : pool) th.join();
+}
+
 void tri_boxes(const HostScene& s, std::vector<float>* box) {
   size_t nt = s.indices.size() / 3;
   box->resize(6 * nt);
-  for (size_t t = 0; t < nt; ++t) {
+  parallel_for(nt, [&](size_t t) {
     const float* a = s.vertices[s.indices[3 * t]].position;
     const float* b = s.vertices[s.indices[3 * t + 1]].position;
     const float* c = s.vertices[s.indices[3 * t + 2]].position;
@@ -754,7 +776,7 @@ void tri_boxes(const HostScene& s, std::vector<float>* box) {
       (*box)[6 * t + k] = std::min(std::min(a[k], b[k]), c[k]);
       (*box)[6 * t + 3 + k] = std::max(std::max(a[k], b[k]), c[k]);
     }
-  }
+  });
 }
 
 int check_tree(const std::vector<nb_bvh_node>& ref, uint32_t root, size_t n_prims) {
@@ -777,6 +799,27 @@ int check_tree(const std::vector<nb_bvh_node>& ref, uint32_t root, size_t n_prim
     stack.emplace_back(node.start + 1, d + 1);
   }
   return NB_OK;
+}
+
+// true if no binary node lies below two of the roots (trees from the reference builder never
+// share nodes; trees handed in through nb_scene_create_from_bvh may)
+bool disjoint_trees(const std::vector<nb_bvh_node>& ref, const std::vector<uint32_t>& roots) {
+  std::vector<uint8_t> seen(ref.size(), 0);
+  std::vector<uint32_t> stack;
+  for (uint32_t root : roots) {
+    stack.assign(1, root);
+    while (!stack.empty()) {
+      const uint32_t n = stack.back();
+      stack.pop_back();
+      if (seen[n]) return false;
+      seen[n] = 1;
+      if (ref[n].end == 0) {
+        stack.push_back(ref[n].start);
+        stack.push_back(ref[n].start + 1);
+      }
+    }
+  }
+  return true;
 }
 
 // world box of an instance: the 8 corners of its BLAS root box through local_to_world
@@ -841,15 +884,22 @@ std::vector<TlasEntry> tlas_entries(const HostScene& s, const std::vector<uint32
 // benchmark frame).  Traversal stays conservative: every box contains its entry's geometry.
 void entry_boxes(const HostScene& s, const std::vector<uint32_t>& tri_order, const std::vector<TlasEntry>& e,
                  std::vector<Prim>* out) {
-  std::map<uint32_t, std::vector<uint32_t>> verts;  // wide node -> vertices below it (sorted, unique)
-  for (const TlasEntry& en : e) {
-    if (verts.count(en.node)) continue;
-    std::vector<uint32_t> v, st{en.node};
+  // the distinct wide nodes the entries start at, and the vertices below each (unique, in
+  // order of first use: only their bounds are taken), gathered in parallel
+  std::map<uint32_t, size_t> node_idx;
+  std::vector<uint32_t> nodes;
+  for (const TlasEntry& en : e)
+    if (node_idx.emplace(en.node, nodes.size()).second) nodes.push_back(en.node);
+  std::vector<std::vector<uint32_t>> verts(nodes.size());
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  auto gather = [&](size_t k, std::vector<uint8_t>& mark) {
+    std::vector<uint32_t>& v = verts[k];
+    std::vector<uint32_t> st{nodes[k]};
     while (!st.empty()) {
       const WideNode& w = s.wblas[st.back()];
       st.pop_back();
-      for (int k = 0; k < w.n_children; ++k) {
-        const uint32_t meta = w.meta[k];
+      for (int c = 0; c < w.n_children; ++c) {
+        const uint32_t meta = w.meta[c];
         if (meta & 0x80u) {
           st.push_back(w.child_base + (meta & 7u));
           continue;
@@ -857,18 +907,32 @@ void entry_boxes(const HostScene& s, const std::vector<uint32_t>& tri_order, con
         const uint32_t first = w.prim_base + (meta & 31u), cnt = meta >> 5;
         for (uint32_t j = 0; j < cnt; ++j) {
           const uint32_t t = tri_order[first + j];
-          for (int q = 0; q < 3; ++q) v.push_back(s.indices[3 * (size_t)t + q]);
+          for (int q = 0; q < 3; ++q) {
+            const uint32_t vi = s.indices[3 * (size_t)t + q];
+            if (!mark[vi]) {
+              mark[vi] = 1;
+              v.push_back(vi);
+            }
+          }
         }
       }
     }
-    std::sort(v.begin(), v.end());
-    v.erase(std::unique(v.begin(), v.end()), v.end());
-    verts.emplace(en.node, std::move(v));
+    for (uint32_t vi : v) mark[vi] = 0;
+  };
+  {
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> pool;
+    for (unsigned w = 0; w < std::min<size_t>(hw, nodes.size()); ++w)
+      pool.emplace_back([&] {
+        std::vector<uint8_t> mark(s.vertices.size(), 0);
+        for (size_t k; (k = next.fetch_add(1)) < nodes.size();) gather(k, mark);
+      });
+    for (std::thread& th : pool) th.join();
   }
   out->assign(e.size(), Prim{});
   auto one = [&](size_t j) {
     const nb_instance& in = s.instances[e[j].inst];
-    const std::vector<uint32_t>& v = verts.at(e[j].node);
+    const std::vector<uint32_t>& v = verts[node_idx.at(e[j].node)];
     Prim& p = (*out)[j];
     p.payload = (uint32_t)j;
     if (v.empty()) {  // no geometry: the transformed root box
@@ -895,7 +959,6 @@ void entry_boxes(const HostScene& s, const std::vector<uint32_t>& tri_order, con
       p.c[r] = (p.mn[r] + p.mx[r]) * 0.5f;
     }
   };
-  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
   std::atomic<size_t> next{0};
   std::vector<std::thread> pool;
   for (unsigned w = 0; w < hw; ++w)
@@ -914,12 +977,15 @@ int to_device_layout(HostScene* s) {
   std::vector<float> tbox;
   tri_boxes(*s, &tbox);
 
-  // BLAS: one wide tree per distinct root; triangles re-ordered per wide tree
+  // BLAS: one wide tree per distinct root (in order of first use); triangles re-ordered per
+  // wide tree.  Disjoint trees are collapsed in parallel into their own arrays and appended in
+  // order, their node and triangle indices moved by the sizes before them: the same arrays as
+  // collapsing them one after the other.
   s->wblas.clear();
   s->wblas_root.clear();
   std::vector<uint32_t> tri_order;
   std::map<uint32_t, uint32_t> root_id;
-  Collapser cb{s->blas, tbox, &s->wblas, &tri_order, 2};
+  std::vector<uint32_t> roots;
   std::vector<uint32_t> inst_blas(n_inst);
   for (size_t i = 0; i < n_inst; ++i) {
     const uint32_t root = s->instances[i].node;
@@ -927,14 +993,44 @@ int to_device_layout(HostScene* s) {
     if (it == root_id.end()) {
       int st = check_tree(s->blas, root, nt);
       if (st) return st;
-      uint32_t id = (uint32_t)s->wblas_root.size();
-      s->wblas_root.push_back(cb.build(root));
-      it = root_id.emplace(root, id).first;
+      it = root_id.emplace(root, (uint32_t)roots.size()).first;
+      roots.push_back(root);
     }
     inst_blas[i] = it->second;
   }
+  std::vector<Collapser::Span> memo(s->blas.size());
+  std::vector<std::vector<WideNode>> wide(roots.size());
+  std::vector<std::vector<uint32_t>> order(roots.size());
+  auto collapse = [&](size_t k) {
+    Collapser cb{s->blas, tbox, &wide[k], &order[k], 2, &memo};
+    cb.build(roots[k]);  // the root is the first node of its array
+  };
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  if (roots.size() > 1 && hw > 1 && disjoint_trees(s->blas, roots)) {
+    std::atomic<size_t> next{0};
+    std::vector<std::thread> pool;
+    for (unsigned w = 0; w < std::min<size_t>(hw, roots.size()); ++w)
+      pool.emplace_back([&] {
+        for (size_t k; (k = next.fetch_add(1)) < roots.size();) collapse(k);
+      });
+    for (std::thread& th : pool) th.join();
+  } else {
+    for (size_t k = 0; k < roots.size(); ++k) collapse(k);
+  }
+  for (size_t k = 0; k < roots.size(); ++k) {
+    const uint32_t node_off = (uint32_t)s->wblas.size(), prim_off = (uint32_t)tri_order.size();
+    s->wblas_root.push_back(node_off);
+    for (WideNode w : wide[k]) {
+      w.child_base += node_off;
+      w.prim_base += prim_off;
+      s->wblas.push_back(w);
+    }
+    tri_order.insert(tri_order.end(), order[k].begin(), order[k].end());
+    std::vector<WideNode>().swap(wide[k]);
+    std::vector<uint32_t>().swap(order[k]);
+  }
   s->tris.assign(tri_order.size(), GpuTri{});
-  for (size_t k = 0; k < tri_order.size(); ++k) {
+  parallel_for(tri_order.size(), [&](size_t k) {
     const uint32_t t = tri_order[k];
     const float* a = s->vertices[s->indices[3 * t]].position;
     const float* b = s->vertices[s->indices[3 * t + 1]].position;
@@ -944,15 +1040,15 @@ int to_device_layout(HostScene* s) {
     g.pad0 = 0;
     g.ref_index = t;
     g.pad2 = 0;
-  }
+  });
   s->vattr.resize(nv);
-  for (size_t i = 0; i < nv; ++i) {
+  parallel_for(nv, [&](size_t i) {
     const nb_vertex& v = s->vertices[i];
     GpuVAttr& g = s->vattr[i];
     for (int k = 0; k < 3; ++k) { g.n[k] = v.normal[k]; g.t[k] = v.tangent[k]; }
     g.tw = v.tangent[3];
     g.pad = 0.0f;
-  }
+  });
 
   // TLAS over the entries (tlas_entries, entry_boxes): the reference's SAH build over their
   // boxes, collapsed like the BLAS; entries re-ordered by the wide TLAS
@@ -973,7 +1069,8 @@ int to_device_layout(HostScene* s) {
     for (size_t k = 0; k < eb.size(); ++k)
       for (int q = 0; q < 3; ++q) { ebox[6 * k + q] = eb[k].mn[q]; ebox[6 * k + 3 + q] = eb[k].mx[q]; }
     std::vector<uint32_t> order;
-    Collapser ct{tlas, ebox, &s->wtlas, &order, 1};
+    std::vector<Collapser::Span> tmemo(tlas.size());
+    Collapser ct{tlas, ebox, &s->wtlas, &order, 1, &tmemo};
     ct.build(0);  // raytracing_sw.wgsl:183-186: the TLAS root is node 0
     s->itrace.assign(order.size(), GpuInstTrace{});
     s->tlas_entries = order.size();
