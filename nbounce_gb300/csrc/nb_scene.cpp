@@ -54,6 +54,26 @@ inline uint32_t as_u32(float x) {
   return (uint32_t)x;
 }
 
+// f(i) for i in [0, n) over up to 16 threads in chunks (f writes only its own elements)
+template <class F>
+void parallel_for(size_t n, F f) {
+  const size_t chunk = 1 << 16;
+  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
+  const size_t n_chunks = (n + chunk - 1) / chunk;
+  if (hw == 1 || n_chunks < 2) {
+    for (size_t i = 0; i < n; ++i) f(i);
+    return;
+  }
+  std::atomic<size_t> next{0};
+  std::vector<std::thread> pool;
+  for (unsigned w = 0; w < std::min<size_t>(hw, n_chunks); ++w)
+    pool.emplace_back([&] {
+      for (size_t c; (c = next.fetch_add(1)) < n_chunks;)
+        for (size_t i = c * chunk, e = std::min(n, i + chunk); i < e; ++i) f(i);
+    });
+  for (std::thread& th : pool) th.join();
+}
+
 struct Prim {
   float c[3];
   float mn[3];
@@ -222,15 +242,47 @@ uint32_t append_tree(std::vector<nb_bvh_node>& nodes, Prim* p, uint32_t s, uint3
 // threshold are split on separate threads.  The reference numbers nodes in the order its
 // right-first DFS splits them (children at len, len + 1); replaying that DFS over the finished
 // structure reproduces the numbering, and the in-place partitions leave the same permutation.
+// Ranges too small to spawn anywhere below them (under 2 kParallelMin primitives, or no spawn
+// depth left) are built by the sequential DFS into a flat array, spliced into the numbering by
+// the replay, instead of one heap node per split.
 struct TreeNode {
   nb_bvh_node n;
   std::unique_ptr<TreeNode> lo, hi;
+  std::vector<nb_bvh_node> flat;  // sequential subtree: flat[0] is n, children at local indices
 };
+
+// append_tree's DFS from an already bounded root at depth0, into a fresh array (root at 0)
+void append_subtree(std::vector<nb_bvh_node>& nodes, Prim* p, const nb_bvh_node& root, uint32_t depth0) {
+  constexpr uint32_t kMaxDepth = 32;
+  nodes.push_back(root);
+  std::vector<std::pair<uint32_t, uint32_t>> stack;
+  stack.emplace_back(depth0, 0u);
+  while (!stack.empty()) {
+    auto [depth, idx] = stack.back();
+    stack.pop_back();
+    if (depth >= kMaxDepth) continue;
+    nb_bvh_node node = nodes[idx];
+    nb_bvh_node lo, hi;
+    if (split_node(p, node, &lo, &hi)) {
+      uint32_t li = (uint32_t)nodes.size();
+      nodes[idx].end = 0;
+      nodes[idx].start = li;
+      nodes.push_back(lo);
+      nodes.push_back(hi);
+      stack.emplace_back(depth + 1, li);
+      stack.emplace_back(depth + 1, li + 1);
+    }
+  }
+}
 
 void split_recursive(Prim* p, TreeNode* t, uint32_t depth, int spawn_depth) {
   constexpr uint32_t kMaxDepth = 32;
   constexpr uint32_t kParallelMin = 1u << 15;
   if (depth >= kMaxDepth) return;
+  if (spawn_depth <= 0 || t->n.end - t->n.start < 2 * kParallelMin) {
+    append_subtree(t->flat, p, t->n, depth);
+    return;
+  }
   nb_bvh_node lo, hi;
   if (!split_node(p, t->n, &lo, &hi)) return;
   t->lo.reset(new TreeNode{lo, nullptr, nullptr});
@@ -254,6 +306,22 @@ uint32_t append_tree_parallel(std::vector<nb_bvh_node>& nodes, Prim* p, uint32_t
   while (!stack.empty()) {
     auto [t, idx] = stack.back();
     stack.pop_back();
+    if (!t->flat.empty()) {
+      // the subtree's DFS numbers its nodes after the current end, in its own order: local
+      // node j (j >= 1) becomes base + j - 1
+      const std::vector<nb_bvh_node>& f = t->flat;
+      if (f.size() > 1) {
+        const uint32_t base = (uint32_t)nodes.size() - 1;
+        nodes[idx].end = 0;
+        nodes[idx].start = base + f[0].start;
+        for (size_t j = 1; j < f.size(); ++j) {
+          nb_bvh_node n = f[j];
+          if (n.end == 0) n.start += base;
+          nodes.push_back(n);
+        }
+      }
+      continue;
+    }
     if (!t->lo) continue;
     uint32_t li = (uint32_t)nodes.size();
     nodes[idx].end = 0;
@@ -274,7 +342,7 @@ int spawn_depth_for(uint32_t n) {
 }
 
 void triangle_cache(const float* pos, size_t pos_stride, const uint32_t* idx, size_t nt, Prim* out) {
-  for (size_t t = 0; t < nt; ++t) {
+  parallel_for(nt, [&](size_t t) {
     const float* a = pos + pos_stride * idx[3 * t];
     const float* b = pos + pos_stride * idx[3 * t + 1];
     const float* c = pos + pos_stride * idx[3 * t + 2];
@@ -285,7 +353,7 @@ void triangle_cache(const float* pos, size_t pos_stride, const uint32_t* idx, si
       q.mx[k] = max_num(max_num(a[k], b[k]), c[k]);
     }
     q.payload = (uint32_t)t;
-  }
+  });
 }
 
 template <class F> void run_parallel(size_t n, F&& fn) {
@@ -744,26 +812,6 @@ struct Collapser {
     return base;
   }
 };
-
-// f(i) for i in [0, n) over up to 16 threads in chunks (f writes only its own elements)
-template <class F>
-void parallel_for(size_t n, F f) {
-  const size_t chunk = 1 << 16;
-  const unsigned hw = std::max(1u, std::min(16u, std::thread::hardware_concurrency()));
-  const size_t n_chunks = (n + chunk - 1) / chunk;
-  if (hw == 1 || n_chunks < 2) {
-    for (size_t i = 0; i < n; ++i) f(i);
-    return;
-  }
-  std::atomic<size_t> next{0};
-  std::vector<std::thread> pool;
-  for (unsigned w = 0; w < std::min<size_t>(hw, n_chunks); ++w)
-    pool.emplace_back([&] {
-      for (size_t c; (c = next.fetch_add(1)) < n_chunks;)
-        for (size_t i = c * chunk, e = std::min(n, i + chunk); i < e; ++i) f(i);
-    });
-  for (std::thread& th : pool) th.join();
-}
 
 void tri_boxes(const HostScene& s, std::vector<float>* box) {
   size_t nt = s.indices.size() / 3;

@@ -18,16 +18,18 @@ def bits(a):
 
 
 @pytest.mark.parametrize("maker", ["soup1", "soup2", "soup3", "soup11", "soup12", "soup5000", "ico4", "hf48",
-                                   "coincident", "grid_ties"])
+                                   "coincident", "grid_ties", "soup300000", "hf256"])
 def test_bvh_build_bit_exact(maker):
+    """The two large cases split their top levels on several threads and the ranges below
+    sequentially into flat arrays spliced into the reference numbering."""
     rng = np.random.default_rng(7)
     if maker.startswith("soup"):
         v, f = scenes.triangle_soup(int(maker[4:]), seed=3)
         pos = v["pos"]
     elif maker == "ico4":
         pos, f = scenes.icosphere(4)
-    elif maker == "hf48":
-        v, f = scenes.heightfield(48, rng)
+    elif maker in ("hf48", "hf256"):
+        v, f = scenes.heightfield(int(maker[2:]), rng)
         pos = v["pos"]
     elif maker == "coincident":
         pos = np.array([[0, 0, 0], [1, 0, 0], [0, 1, 0], [0, 0, 1]], np.float32)
