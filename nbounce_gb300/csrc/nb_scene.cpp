@@ -469,25 +469,34 @@ int build_scene_reference(const nb_vertex* vertices, size_t nv, const uint32_t* 
     }
   }
 
-  // concatenate in primitive order (BVHTree::append numbering) and assemble instances
-  out->blas.clear();
+  // concatenate in primitive order (BVHTree::append numbering): the offsets first, then the
+  // trees copied into place in parallel; then assemble the instances
   std::vector<uint32_t> root_of(np);
   std::vector<Prim> bounds(np);
   std::vector<nb_instance> raw(np);
+  size_t total = 0;
   for (size_t k = 0; k < np; ++k) {
-    uint32_t root;
     if (dedup && first_of[k] != k) {
-      root = root_of[first_of[k]];
+      root_of[k] = root_of[first_of[k]];
     } else {
-      uint32_t off = (uint32_t)out->blas.size();
-      for (nb_bvh_node n : local[k]) {
-        if (n.end == 0) n.start += off;
-        out->blas.push_back(n);
-      }
-      root = off;
-      std::vector<nb_bvh_node>().swap(local[k]);
+      root_of[k] = (uint32_t)total;
+      total += local[k].size();
     }
-    root_of[k] = root;
+  }
+  out->blas.assign(total, nb_bvh_node{});
+  run_parallel(np, [&](size_t k) {
+    if (dedup && first_of[k] != k) return;
+    const uint32_t off = root_of[k];
+    nb_bvh_node* dst = out->blas.data() + off;
+    for (size_t j = 0; j < local[k].size(); ++j) {
+      nb_bvh_node n = local[k][j];
+      if (n.end == 0) n.start += off;
+      dst[j] = n;
+    }
+    std::vector<nb_bvh_node>().swap(local[k]);
+  });
+  for (size_t k = 0; k < np; ++k) {
+    const uint32_t root = root_of[k];
     const nb_primitive& pr = prims[k];
     nb_instance& in = raw[k];
     std::memcpy(in.local_to_world, pr.local_to_world, 64);
@@ -525,8 +534,9 @@ int build_scene_reference(const nb_vertex* vertices, size_t nv, const uint32_t* 
   out->instances.resize(np);
   for (size_t k = 0; k < np; ++k) out->instances[k] = raw[bounds[k].payload];
   out->indices.assign(indices, indices + ni);
-  for (size_t t = 0; t < nt; ++t)
+  parallel_for(nt, [&](size_t t) {
     for (int k = 0; k < 3; ++k) out->indices[3 * t + k] = indices[3 * tris[t].payload + k];
+  });
   out->build_ms = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
   return NB_OK;
 }
