@@ -202,7 +202,8 @@ void nb_env_destroy(nb_env* env);
 int nb_env_create_dds(const void* bytes, size_t n, nb_env** out);
 /* BC6H block decoding on the device, host buffers in and out: blocks holds layers x
  * ceil(height / 4) x ceil(width / 4) 16-byte blocks in row-major block order; out receives
- * layers x height x width RGBA32F texels (alpha 1).  is_signed: 0 = BC6H_UF16, 1 = BC6H_SF16. */
+ * layers x height x width RGBA32F texels (alpha 1).  is_signed: 0 = BC6H_UF16, 1 = BC6H_SF16.
+ * Width, height and layers up to 65536 each (NB_ERR_INVALID_ARG beyond). */
 int nb_bc6h_decode(const void* blocks, uint32_t width, uint32_t height, uint32_t layers, uint32_t is_signed,
                    float* out);
 

@@ -445,7 +445,8 @@ int nb_bc6h_decode(const void* blocks, uint32_t width, uint32_t height, uint32_t
   if (is_signed > 1) return fail(NB_ERR_INVALID_ARG, "is_signed must be 0 or 1");
   if (width == 0 || height == 0 || layers == 0) return NB_OK;
   if (!blocks || !out) return fail(NB_ERR_INVALID_ARG, "NULL argument");
-  if (width > 65536 || height > 65536) return fail(NB_ERR_INVALID_ARG, "BC6H size %u x %u", width, height);
+  if (width > 65536 || height > 65536 || layers > 65536)
+    return fail(NB_ERR_INVALID_ARG, "BC6H size %u x %u x %u layers", width, height, layers);
   int st = check_device();
   if (st) return st;
   const size_t in_bytes = (size_t)((width + 3) / 4) * ((height + 3) / 4) * layers * 16;

@@ -131,3 +131,18 @@ def test_bc6h_writer_takes_block_arrays_of_any_integer_type():
     want = dds.write_cube_dds_bc6h(blocks, 8)
     assert dds.write_cube_dds_bc6h(blocks.view(np.uint32), 8) == want
     assert dds.write_cube_dds_bc6h(blocks.view(np.uint64).reshape(6, -1), 8) == want
+
+
+def test_bc6h_decode_rejects_bad_arguments_before_touching_the_device():
+    import ctypes as C
+
+    from nbounce_gb300 import _lib as L
+    lib = L.lib()
+    blk = np.zeros(16, np.uint8)
+    out = np.zeros(64, np.float32)
+    p_in, p_out = blk.ctypes.data_as(C.c_void_p), out.ctypes.data_as(C.c_void_p)
+    assert lib.nb_bc6h_decode(p_in, 4, 4, 1, 2, p_out) == L.NB_ERR_INVALID_ARG          # is_signed
+    assert lib.nb_bc6h_decode(None, 4, 4, 1, 0, p_out) == L.NB_ERR_INVALID_ARG          # NULL blocks
+    assert lib.nb_bc6h_decode(p_in, 70000, 4, 1, 0, p_out) == L.NB_ERR_INVALID_ARG      # width
+    assert lib.nb_bc6h_decode(p_in, 4, 4, 1 << 20, 0, p_out) == L.NB_ERR_INVALID_ARG    # layers
+    assert lib.nb_bc6h_decode(p_in, 0, 4, 1, 0, p_out) == L.NB_OK                       # nothing to do
