@@ -111,7 +111,8 @@ typedef struct nb_env_desc {
   const float* texels;     /* NB_ENV_EQUIRECT: height rows of width RGBA32F texels (host);
                               NB_ENV_CUBE: 6 faces (+X, -X, +Y, -Y, +Z, -Z: the layer order
                               of the reference's cube texture, texture.rs:89-144) of height
-                              rows of width texels each, width == height */
+                              rows of width texels each, width == height; at most 32768
+                              texels per side */
   uint32_t width, height;
 } nb_env_desc;
 

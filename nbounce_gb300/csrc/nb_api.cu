@@ -349,6 +349,9 @@ int nb_env_create(const nb_env_desc* desc, nb_env** out) {
     return fail(NB_ERR_INVALID_ARG, "unknown environment kind %u", desc->kind);
   if (desc->kind == NB_ENV_CUBE && desc->width != desc->height)
     return fail(NB_ERR_INVALID_ARG, "cube faces must be square (%u x %u)", desc->width, desc->height);
+  if (desc->kind != NB_ENV_CONSTANT && (desc->width > 32768 || desc->height > 32768))
+    return fail(NB_ERR_INVALID_ARG, "environment of %u x %u texels (32768 at most per side)", desc->width,
+                desc->height);
   int st = check_device();
   if (st) return st;
   nb_env* e = new (std::nothrow) nb_env();

@@ -68,3 +68,17 @@ def test_cube_from_equirect_samples_the_same_sky():
     b = O.env_lookup(d, texels=sky)
     # nearest texel against bilinear of the same smooth field
     assert np.median(np.abs(a - b) / (np.abs(b) + 1e-3)) < 0.05
+
+
+def test_oversized_environments_are_rejected_before_touching_the_device():
+    import ctypes as C
+
+    from nbounce_gb300 import _lib as L
+    texel = np.zeros(4, np.float32)
+    for kind, w, h in ((L.NB_ENV_EQUIRECT, 40000, 2), (L.NB_ENV_CUBE, 40000, 40000), (L.NB_ENV_EQUIRECT, 2, 1 << 31)):
+        d = L.NbEnvDesc()
+        d.kind, d.width, d.height = kind, w, h
+        d.texels = texel.ctypes.data
+        h_ = C.c_void_p()
+        assert L.lib().nb_env_create(C.byref(d), C.byref(h_)) == L.NB_ERR_INVALID_ARG
+        assert not h_.value
