@@ -874,6 +874,7 @@ int nb_trace_rays(const nb_scene* scene, const float* rays, size_t n, uint32_t f
 int nb_trace_rays_host(const nb_scene* scene, const float* rays, size_t n, uint32_t flags, float* hits,
                        uint32_t* instances, void* stream) {
   if (!scene || (n && (!rays || !hits))) return fail(NB_ERR_INVALID_ARG, "NULL argument");
+  if (n > 0xFFFFFFE0ull) return fail(NB_ERR_INVALID_ARG, "too many rays in one call");
   if (!scene->uploaded) return fail(NB_ERR_INVALID_ARG, "scene was built with NB_SCENE_HOST_ONLY");
   cudaStream_t st = (cudaStream_t)stream;
   DeviceArena tmp;
