@@ -4,7 +4,7 @@
  * This library is a drop-in for the reference's path-tracing compute pass
  * (julcst/nbounce, src/pathtracing/pathtracer.rs + pathtracing.wgsl + raytracing_sw.wgsl +
  * common.wgsl, with the scene/BVH assembly of src/pathtracing/scene.rs and bvh.rs).
- * A Rust caller binds these symbols with an `extern "C"` block (see INTEGRATION.md).
+ * A Rust caller binds these symbols with an `extern "C"` block.
  *
  * Conventions
  *  - Every entry point returns an nb_status; NB_OK is 0.  On error, nb_last_error() returns a
@@ -309,10 +309,14 @@ int nb_scene_status(const nb_scene* scene, uint32_t* status, void* stream);
  * that cannot allocate device memory while they render (an engine that owns all GPU memory
  * through its own allocator, a real-time loop whose footprint must stay fixed).  All scratch
  * lives in one static device array of 34.9 MB reserved per GPU at library load; images above
- * 262,144 pixels are rejected with NB_ERR_INVALID_ARG.  The first call on a device looks up
- * that array and uploads the Sobol table - make it before any stream capture.  Calls share
- * the array (it keeps the last call's contents); calls that overlap on the GPU race.
- * Synchronises stream.  No counterpart in the reference. */
+ * 262,144 pixels are rejected with NB_ERR_INVALID_ARG.  The first call on a device does a
+ * one-time set-up there (looks up that array's device address and uploads the Sobol table
+ * into it, synchronously), so make that first call before any stream capture begins.  Every
+ * call checks that the array still holds the table and repeats the set-up if not (after a
+ * device reset the module is reloaded and its arrays start zeroed); scenes and environments
+ * do not survive a device reset and must be created again.  Calls share the array (it keeps
+ * the last call's contents); calls that overlap on the GPU race on it.  Synchronises stream.
+ * No counterpart in the reference. */
 int nb_render_static(const nb_scene* scene, const nb_env* env, const nb_camera* camera, uint32_t width,
                      uint32_t height, uint32_t first_sample, uint32_t n_samples, uint32_t bounces,
                      float contribution_factor, float* out_rgba, void* stream);

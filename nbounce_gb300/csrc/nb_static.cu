@@ -10,10 +10,13 @@
 // Limit: at most kStaticPaths = 262,144 paths per wave, so images of at most 262,144 pixels
 // (512 x 512); samples run in waves of floor(262,144 / pixels) samples.  The array is 34.9 MB.
 // Its device address is looked up once per device, with that device current, on the first
-// call there (cudaGetSymbolAddress; the same call uploads the Sobol table) - make that first
-// call before any stream capture.  Every call shares the array and it keeps the last call's
-// contents; the kernels reset what must start at zero.  Calls whose work overlaps on the GPU
-// (other streams, other host threads) race on the array: serialise them.
+// call there (cudaGetSymbolAddress; the same call uploads the Sobol table and a marker word
+// behind it) - make that first call before any stream capture begins.  Every later call looks
+// the address up again and reads the marker back; if either changed (a device reset reloads
+// the module, whose arrays then start zeroed) it repeats the set-up.  Every call shares the
+// array and it keeps the last call's contents; the kernels reset what must start at zero.
+// Calls whose work overlaps on the GPU (other streams, other host threads) race on the array:
+// serialise them.
 
 #include <cstring>
 #include <mutex>
@@ -27,7 +30,11 @@ constexpr size_t kQueueBytes = (size_t)kStaticPaths * 16;                 // one
 constexpr size_t kInstBytes = (size_t)kStaticPaths * 4;                   // hit instance ids
 constexpr size_t kCounterBytes = 1024;                                    // counts, fetch, status, rays
 constexpr size_t kSobolBytes = (size_t)nb::kMaxSampleCount * nb::kLdsStride * 16;
-constexpr size_t kScratchBytes = 8 * kQueueBytes + kInstBytes + kCounterBytes + kSobolBytes;
+constexpr size_t kMarkerBytes = 256;                                      // set-up marker
+constexpr size_t kSobolOffset = 8 * kQueueBytes + kInstBytes + kCounterBytes;
+constexpr size_t kMarkerOffset = kSobolOffset + kSobolBytes;
+constexpr size_t kScratchBytes = kMarkerOffset + kMarkerBytes;
+constexpr unsigned long long kMarker = 0x6E625F7374617469ull;              // written after the table
 
 static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
@@ -37,25 +44,36 @@ unsigned char* g_base[kMaxDevices];    // device ordinal -> device address of g_
 nb::WaveTables g_tables;               // host staging of the kernel parameter tables
 float g_table_host[(size_t)nb::kMaxSampleCount * nb::kLdsStride * 4];  // Sobol table staging
 
-// Device address of the scratch array on the current device; first call per device looks it
-// up and uploads the Sobol table.
-int scratch_base(unsigned char** out) {
+// Device address of the scratch array on the current device.  The first call per device
+// looks it up and uploads the Sobol table and the marker; later calls check that the address
+// and the marker are unchanged (one 8-byte read on the caller's stream) and redo the set-up
+// otherwise.
+int scratch_base(cudaStream_t st, unsigned char** out) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return nb::cuda_fail(e, "cudaGetDevice");
   if (dev < 0 || dev >= kMaxDevices) return nb::fail(NB_ERR_INVALID_ARG, "device ordinal %d out of range", dev);
-  if (g_base[dev]) {
-    *out = g_base[dev];
-    return NB_OK;
-  }
   void* p = nullptr;
   e = cudaGetSymbolAddress(&p, g_scratch);
   if (e != cudaSuccess) return nb::cuda_fail(e, "cudaGetSymbolAddress(static scratch)");
-  nb::sobol_burley_table(nb::kMaxSampleCount, nb::kLdsStride, 0, g_table_host);
   unsigned char* base = (unsigned char*)p;
-  e = cudaMemcpy(base + 8 * kQueueBytes + kInstBytes + kCounterBytes, g_table_host, kSobolBytes,
-                 cudaMemcpyHostToDevice);
+  if (g_base[dev] == base) {
+    unsigned long long mark = 0;
+    e = cudaMemcpyAsync(&mark, base + kMarkerOffset, sizeof(mark), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return nb::cuda_fail(e, "static scratch marker read");
+    if (mark == kMarker) {
+      *out = base;
+      return NB_OK;
+    }
+  }
+  g_base[dev] = nullptr;
+  nb::sobol_burley_table(nb::kMaxSampleCount, nb::kLdsStride, 0, g_table_host);
+  e = cudaMemcpy(base + kSobolOffset, g_table_host, kSobolBytes, cudaMemcpyHostToDevice);
   if (e != cudaSuccess) return nb::cuda_fail(e, "cudaMemcpy(Sobol table)");
+  const unsigned long long mark = kMarker;
+  e = cudaMemcpy(base + kMarkerOffset, &mark, sizeof(mark), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return nb::cuda_fail(e, "cudaMemcpy(static scratch marker)");
   g_base[dev] = base;
   *out = base;
   return NB_OK;
@@ -79,10 +97,10 @@ extern "C" int nb_render_static(const nb_scene* scene, const nb_env* env, const 
   if (bounces + 2 > kMaxBounceSlots) return fail(NB_ERR_INVALID_ARG, "bounces must be <= %u", kMaxBounceSlots - 2);
   if (n_samples == 0) return NB_OK;
   std::lock_guard<std::mutex> lk(g_mu);
-  unsigned char* base = nullptr;
-  int rc = scratch_base(&base);
-  if (rc) return rc;
   cudaStream_t st = (cudaStream_t)stream;
+  unsigned char* base = nullptr;
+  int rc = scratch_base(st, &base);
+  if (rc) return rc;
 
   PathBatch pb{};
   float4* q = (float4*)base;
@@ -97,7 +115,7 @@ extern "C" int nb_render_static(const nb_scene* scene, const nb_env* env, const 
   pb.fetch = counters + kMaxBounceSlots;
   pb.status = counters + 2 * kMaxBounceSlots;
   unsigned long long* rays = (unsigned long long*)(counters + 2 * kMaxBounceSlots + 2);
-  pb.sobol = (const float4*)(base + 8 * kQueueBytes + kInstBytes + kCounterBytes);
+  pb.sobol = (const float4*)(base + kSobolOffset);
   pb.sobol_entries = kMaxSampleCount * kLdsStride;
   cudaError_t e = cudaMemsetAsync(pb.status, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return cuda_fail(e, "cudaMemsetAsync");

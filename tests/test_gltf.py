@@ -1,7 +1,8 @@
 """GLB ingest (Scene::parse_gltf, scene.rs:108-217).
 
 The reference's own scenes (assets/spheres.glb, assets/testscene.glb) are parsed when the
-reference tree is mounted (this is a CPU test; it skips elsewhere); a generated scene is
+directory holding them is named by the NB_REFERENCE_ASSETS environment variable (a CPU test;
+it skips without it); a generated scene is
 round-tripped through write_glb/parse_glb everywhere, and the MeshError cases are checked.
 """
 import json
@@ -15,13 +16,13 @@ import nbounce_gb300 as nb
 from nbounce_gb300 import gltf, scenes
 from oracle import oracle as O
 
-REF_ASSETS = "/root/reference/assets"
+REF_ASSETS = os.environ.get("NB_REFERENCE_ASSETS", "")
 
 
 def asset(name):
-    p = os.path.join(REF_ASSETS, name)
-    if not os.path.exists(p):
-        pytest.skip("reference assets not mounted")
+    p = os.path.join(REF_ASSETS, name) if REF_ASSETS else ""
+    if not p or not os.path.exists(p):
+        pytest.skip("NB_REFERENCE_ASSETS does not name the reference's assets directory")
     return p
 
 
