@@ -37,7 +37,10 @@ typedef enum nb_status {
   NB_ERR_TIMEOUT = 4,         /* a bounded device loop gave up (traversal iteration cap) */
   NB_ERR_STACK_OVERFLOW = 5,  /* a traversal stack overflowed; results of that launch are suspect */
   NB_ERR_NO_DEVICE = 6,       /* no CUDA device is available */
-  NB_ERR_EXHAUSTED = 7        /* the Sobol table has no rows left (sample >= max_sample_count) */
+  NB_ERR_EXHAUSTED = 7,       /* the Sobol table has no rows left (sample >= max_sample_count) */
+  NB_ERR_BUSY = 8,            /* the render-job server's queue is full: the job was not queued */
+  NB_ERR_CANCELLED = 9,       /* the job was cancelled (nb_server_cancel) */
+  NB_ERR_EXPIRED = 10         /* the job's deadline passed before it finished */
 } nb_status;
 
 /* ---------------------------------------------------------------------------------------
@@ -265,6 +268,27 @@ int nb_pathtracer_enable_timing(nb_pathtracer* pt, int enable);
 /* Sums the recorded launch times (synchronises stream); reset != 0 clears the record. */
 int nb_pathtracer_kernel_times(nb_pathtracer* pt, nb_kernel_times* out, int reset, void* stream);
 
+/* Traversal work counters, per bounce: what the device's own layout fetches for the closest-hit
+ * queries of that bounce - 80-byte 8-wide nodes (TLAS and BLAS), 48-byte triangle records,
+ * 64-byte instance records - and the 8-byte stack entries pushed (each popped once).  While
+ * enabled, renders run an instrumented copy of the traversal kernel (same results, slower);
+ * the measurement counterpart of the reference's n_aabb / n_tri counters
+ * (raytracing_sw.wgsl:187,207-208,261,280).  Off by default; no counterpart in the reference's
+ * API. */
+typedef struct nb_trace_counters {
+  uint64_t rays;                 /* closest-hit queries traced */
+  uint64_t tlas_node_tests;      /* 8-wide TLAS nodes tested */
+  uint64_t blas_node_tests;      /* 8-wide BLAS nodes tested */
+  uint64_t triangle_tests;       /* Moller-Trumbore tests */
+  uint64_t instance_entries;     /* world-to-local ray transforms */
+  uint64_t stack_pushes;         /* traversal stack entries written */
+} nb_trace_counters;
+int nb_pathtracer_enable_trace_counters(nb_pathtracer* pt, int enable);
+/* Copies the counters of bounces 0 .. n_bounces-1 since the last reset into out[0 .. n_bounces-1]
+ * (synchronises stream); reset != 0 clears them. */
+int nb_pathtracer_trace_counters(nb_pathtracer* pt, nb_trace_counters* out, uint32_t n_bounces, int reset,
+                                 void* stream);
+
 /* Estimator options.  0 (default) is the reference's: BSDF sampling only, the environment
  * reached only by rays that escape.  NB_SAMPLE_ENV_NEE adds next-event estimation toward the
  * environment (the reference's README lists environment importance sampling as planned work,
@@ -357,6 +381,8 @@ typedef struct nb_job_desc {
   uint32_t bounces;
   float contribution_factor;
   uint32_t flags;               /* NB_JOB_* options (0: the reference estimator) */
+  uint32_t deadline_ms;         /* 0: none; else the job fails with NB_ERR_EXPIRED if it has not
+                                   finished this long after its submission (checked between waves) */
   float* host_out;              /* optional: width*height RGBA32F copied here when done */
 } nb_job_desc;
 
@@ -371,7 +397,12 @@ typedef struct nb_server_stats {
   uint64_t rays;                /* traversal queries of all waves so far */
   double gpu_busy_ms;           /* sum of wave durations (CUDA events) */
   uint64_t bytes_in_use, peak_bytes_in_use, budget_bytes;
-  uint32_t queued, active;
+  uint32_t queued, active;      /* waiting for admission / admitted and unfinished */
+  uint64_t jobs_rejected;       /* submissions refused with NB_ERR_BUSY (not counted as submitted) */
+  uint64_t jobs_cancelled;      /* finished with NB_ERR_CANCELLED (also counted in jobs_failed) */
+  uint64_t jobs_expired;        /* finished with NB_ERR_EXPIRED (also counted in jobs_failed) */
+  uint32_t queue_limit;         /* nb_server_set_queue_limit (0: none) */
+  uint32_t reserved;
 } nb_server_stats;
 
 /* hbm_budget_bytes bounds the server's device memory (path buffers + job images);
@@ -387,13 +418,28 @@ int nb_server_add_env(nb_server* server, const nb_env* env, uint32_t* slot);
 struct nb_cache_config; /* defined with the radiance cache API below */
 int nb_server_set_cache_config(nb_server* server, const struct nb_cache_config* cfg);
 /* Queues a job; thread-safe, returns at once.  NB_ERR_INVALID_ARG for bad slots or sizes,
- * NB_ERR_OOM if the job can never fit the budget. */
+ * NB_ERR_OOM if the job can never fit the budget, NB_ERR_BUSY if the queue limit is reached
+ * (load shedding: the caller may retry later). */
 int nb_server_submit(nb_server* server, const nb_job_desc* job, uint64_t* job_id);
+/* Admission beyond saturation: at most max_queued jobs wait for admission (0, the default:
+ * no limit, so above the GPU's throughput the queue and the latency grow without bound);
+ * submissions beyond the limit return NB_ERR_BUSY at once.  Thread-safe. */
+int nb_server_set_queue_limit(nb_server* server, uint32_t max_queued);
+/* Cancels an unfinished job: a queued job leaves the queue; an admitted job gets no further
+ * waves, its waves already on the GPU run to completion and its image is freed after them.
+ * The job then finishes with NB_ERR_CANCELLED (nb_server_wait reports it) and every other
+ * job's image is unchanged.  NB_ERR_INVALID_ARG for an unknown or already finished job. */
+int nb_server_cancel(nb_server* server, uint64_t job_id);
+/* Test hook for the allocation failure path: the nth job-image allocation from now on
+ * (n >= 1; 0 disarms) fails as cudaMallocAsync does when device memory runs out, so that job
+ * finishes with NB_ERR_OOM while the others go on, without exhausting the device. */
+int nb_server_fail_alloc(nb_server* server, uint32_t nth);
 /* Waits up to timeout_ms (< 0: forever) for a job; NB_ERR_TIMEOUT if it is not done yet. */
 int nb_server_wait(nb_server* server, uint64_t job_id, int timeout_ms, nb_job_info* info);
 /* Copies a finished job's image (when it was submitted without host_out) and frees it. */
 int nb_server_fetch(nb_server* server, uint64_t job_id, float* host_rgba);
-/* Forgets a finished job's record. */
+/* Forgets a finished job's record (a failed job's record is kept internally until its waves
+ * still on the GPU have finished). */
 int nb_server_release(nb_server* server, uint64_t job_id);
 int nb_server_get_stats(nb_server* server, nb_server_stats* stats);
 /* Finishes the queued and active jobs, then stops the scheduler and frees its memory. */

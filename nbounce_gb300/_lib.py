@@ -18,6 +18,9 @@ NB_ERR_TIMEOUT = 4
 NB_ERR_STACK_OVERFLOW = 5
 NB_ERR_NO_DEVICE = 6
 NB_ERR_EXHAUSTED = 7
+NB_ERR_BUSY = 8
+NB_ERR_CANCELLED = 9
+NB_ERR_EXPIRED = 10
 
 NB_SCENE_DEDUP_MESHES = 1
 NB_SCENE_HOST_ONLY = 2
@@ -68,6 +71,11 @@ class NbKernelTimes(C.Structure):
                 ("cache_train_launches", C.c_uint64)]
 
 
+class NbTraceCounters(C.Structure):
+    _fields_ = [("rays", C.c_uint64), ("tlas_node_tests", C.c_uint64), ("blas_node_tests", C.c_uint64),
+                ("triangle_tests", C.c_uint64), ("instance_entries", C.c_uint64), ("stack_pushes", C.c_uint64)]
+
+
 NB_CACHE_PARAMS = 21504
 NB_CACHE_TCGEN05 = 0
 NB_CACHE_MMA_SYNC = 1
@@ -92,7 +100,8 @@ class NbCacheStats(C.Structure):
 class NbJobDesc(C.Structure):
     _fields_ = [("scene", C.c_uint32), ("env", C.c_uint32), ("camera", NbCamera), ("width", C.c_uint32),
                 ("height", C.c_uint32), ("spp", C.c_uint32), ("bounces", C.c_uint32),
-                ("contribution_factor", C.c_float), ("flags", C.c_uint32), ("host_out", C.c_void_p)]
+                ("contribution_factor", C.c_float), ("flags", C.c_uint32), ("deadline_ms", C.c_uint32),
+                ("host_out", C.c_void_p)]
 
 
 class NbJobInfo(C.Structure):
@@ -104,7 +113,9 @@ class NbServerStats(C.Structure):
     _fields_ = [("jobs_submitted", C.c_uint64), ("jobs_done", C.c_uint64), ("jobs_failed", C.c_uint64),
                 ("waves", C.c_uint64), ("rays", C.c_uint64), ("gpu_busy_ms", C.c_double),
                 ("bytes_in_use", C.c_uint64), ("peak_bytes_in_use", C.c_uint64), ("budget_bytes", C.c_uint64),
-                ("queued", C.c_uint32), ("active", C.c_uint32)]
+                ("queued", C.c_uint32), ("active", C.c_uint32), ("jobs_rejected", C.c_uint64),
+                ("jobs_cancelled", C.c_uint64), ("jobs_expired", C.c_uint64), ("queue_limit", C.c_uint32),
+                ("reserved", C.c_uint32)]
 
 
 class NbError(RuntimeError):
@@ -157,6 +168,8 @@ def lib():
         "nb_pathtracer_set_batch_paths": ([vp, u32], i32),
         "nb_pathtracer_enable_timing": ([vp, i32], i32),
         "nb_pathtracer_kernel_times": ([vp, vp, i32, vp], i32),
+        "nb_pathtracer_enable_trace_counters": ([vp, i32], i32),
+        "nb_pathtracer_trace_counters": ([vp, vp, u32, i32, vp], i32),
         "nb_trace_rays": ([vp, vp, sz, u32, vp, vp, vp], i32),
         "nb_trace_rays_host": ([vp, vp, sz, u32, vp, vp, vp], i32),
         "nb_render_static": ([vp, vp, vp, u32, u32, u32, u32, u32, C.c_float, vp, vp], i32),
@@ -169,6 +182,9 @@ def lib():
         "nb_server_fetch": ([vp, u64, vp], i32),
         "nb_server_release": ([vp, u64], i32),
         "nb_server_get_stats": ([vp, vp], i32),
+        "nb_server_set_queue_limit": ([vp, u32], i32),
+        "nb_server_cancel": ([vp, u64], i32),
+        "nb_server_fail_alloc": ([vp, u32], i32),
         "nb_server_destroy": ([vp], None),
         "nb_cache_default_config": ([vp], None),
         "nb_cache_create": ([vp, vp], i32),

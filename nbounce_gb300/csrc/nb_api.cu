@@ -66,6 +66,9 @@ struct nb_pathtracer {
   uint32_t shadow_capacity = 0;
   ShadowQueue sq{};
   int sms = 1;
+  // optional traversal work counters (instrumented trace kernel), 8 per bounce slot
+  DeviceArena counter_mem;
+  unsigned long long* d_trace_counts = nullptr;
   // optional per-kernel event timing: (kind, start, stop) of every recorded launch
   bool timing = false;
   std::vector<cudaEvent_t> event_pool;
@@ -159,6 +162,9 @@ const char* nb_status_string(int status) {
     case NB_ERR_STACK_OVERFLOW: return "NB_ERR_STACK_OVERFLOW";
     case NB_ERR_NO_DEVICE: return "NB_ERR_NO_DEVICE";
     case NB_ERR_EXHAUSTED: return "NB_ERR_EXHAUSTED";
+    case NB_ERR_BUSY: return "NB_ERR_BUSY";
+    case NB_ERR_CANCELLED: return "NB_ERR_CANCELLED";
+    case NB_ERR_EXPIRED: return "NB_ERR_EXPIRED";
     default: return "unknown status";
   }
 }
@@ -555,6 +561,7 @@ void nb_pathtracer_destroy(nb_pathtracer* pt) {
   pt->tables.release();
   pt->image.release();
   pt->shadow.release();
+  pt->counter_mem.release();
   delete pt;
 }
 
@@ -668,7 +675,9 @@ static int render_samples(nb_pathtracer* pt, const nb_scene* scene, const nb_cam
     }
     cudaError_t e = timed_launch(pt, kKindRaygen, st, [&] { return launch_raygen(pb, wt, pt->sms, st); });
     for (uint32_t b = 0; b <= B && e == cudaSuccess; ++b) {
-      e = timed_launch(pt, kKindTrace, st, [&] { return launch_trace_wave(pb, wt, true, b, pt->d_rays, pt->sms, st); });
+      e = timed_launch(pt, kKindTrace, st, [&] {
+        return launch_trace_wave(pb, wt, true, b, pt->d_rays, pt->sms, st, pt->d_trace_counts);
+      });
       if (e == cudaSuccess)
         e = timed_launch(pt, kKindShade, st, [&] {
           if (pt->cache) return launch_shade_cache(pb, wt, cw, b, pt->sms, st);
@@ -745,6 +754,41 @@ int nb_pathtracer_kernel_times(nb_pathtracer* pt, nb_kernel_times* out, int rese
     }
     pt->timed.clear();
   }
+  return NB_OK;
+}
+
+int nb_pathtracer_enable_trace_counters(nb_pathtracer* pt, int enable) {
+  if (!pt) return fail(NB_ERR_INVALID_ARG, "NULL argument");
+  if (!enable) {
+    pt->counter_mem.release();
+    pt->d_trace_counts = nullptr;
+    return NB_OK;
+  }
+  if (pt->d_trace_counts) return NB_OK;
+  void* p = nullptr;
+  const size_t bytes = 8 * kMaxBounceSlots * sizeof(unsigned long long);
+  int rc = pt->counter_mem.alloc(bytes, &p);
+  if (rc) return rc;
+  NB_CUDA(cudaMemset(p, 0, bytes), "cudaMemset(trace counters)");
+  pt->d_trace_counts = (unsigned long long*)p;
+  return NB_OK;
+}
+
+int nb_pathtracer_trace_counters(nb_pathtracer* pt, nb_trace_counters* out, uint32_t n_bounces, int reset,
+                                 void* stream) {
+  if (!pt || (!out && n_bounces)) return fail(NB_ERR_INVALID_ARG, "NULL argument");
+  if (!pt->d_trace_counts) return fail(NB_ERR_INVALID_ARG, "trace counters are not enabled");
+  if (n_bounces > kMaxBounceSlots) return fail(NB_ERR_INVALID_ARG, "at most %u bounce slots", kMaxBounceSlots);
+  cudaStream_t st = (cudaStream_t)stream;
+  std::vector<unsigned long long> h(8 * kMaxBounceSlots);
+  NB_CUDA(cudaMemcpyAsync(h.data(), pt->d_trace_counts, h.size() * sizeof(h[0]), cudaMemcpyDeviceToHost, st),
+          "cudaMemcpyAsync(trace counters)");
+  NB_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+  for (uint32_t b = 0; b < n_bounces; ++b) {
+    const unsigned long long* c = h.data() + 8 * b;
+    out[b] = nb_trace_counters{c[5], c[0], c[1], c[2], c[3], c[4]};
+  }
+  if (reset) NB_CUDA(cudaMemsetAsync(pt->d_trace_counts, 0, h.size() * sizeof(h[0]), st), "cudaMemsetAsync");
   return NB_OK;
 }
 

@@ -106,11 +106,18 @@ __device__ __forceinline__ void trace_begin(TraceState& t, uint2* stack, const D
   t.iter = 0;
 }
 
+// Work counters of the instrumented traversal (kCount instantiations only): what the device
+// layout fetches per ray - 80-byte wide nodes of the TLAS and the BLASes, 48-byte triangle
+// records, 64-byte instance records - and the 8-byte stack entries pushed (each later popped).
+struct TraceCount {
+  uint32_t tlas_nodes = 0, blas_nodes = 0, tris = 0, insts = 0, pushes = 0;
+};
+
 // One traversal step: pop the next entry when no node is pending, then test one 8-wide node
 // and its leaf triangles.  Returns false once the ray is finished (stack empty, an any-hit
 // found, or the iteration cap reached).
-template <bool kAny>
-__device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const DevScene& s) {
+template <bool kAny, bool kCount = false>
+__device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const DevScene& s, TraceCount* cnt = nullptr) {
   if (t.iter > kIterationCap) {
     t.status |= kStatusIterationCap;
     return false;
@@ -139,6 +146,7 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
       if (__uint_as_float(e.y) >= h_t) continue;  // raytracing_sw.wgsl:197,271
       if (!in_blas && (e.x & kInstanceBit)) {
         // enter an instance: transform the world ray (raytracing_sw.wgsl:202-206)
+        if (kCount) ++cnt->insts;
         const float4* it = s.inst_trace + 4 * (size_t)(e.x & ~kInstanceBit);
         const float4 r0 = ld4(it), r1 = ld4(it + 1), r2 = ld4(it + 2), r3 = ld4(it + 3);
         ro = V3{r0.x * wo.x + r0.y * wo.y + r0.z * wo.z + r0.w * 1.0f,
@@ -161,6 +169,7 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
   have_node = false;
 
   // ---- one 8-wide node: quantised slab tests of all children ----
+  if (kCount) ++(in_blas ? cnt->blas_nodes : cnt->tlas_nodes);
   const float4* np = (in_blas ? s.blas_wide : s.tlas_wide) + 5 * (size_t)node;
   const float4 q0 = ld4(np), q1 = ld4(np + 1), q2 = ld4(np + 2), q3 = ld4(np + 3), q4 = ld4(np + 4);
   const uint32_t eb = f2u(q0.w);
@@ -252,6 +261,7 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
     } else if (sp < kStackSize) {
       stack[sp] = make_uint2(ref, kk & ~7u);
       ++sp;
+      if (kCount) ++cnt->pushes;
     } else {
       status |= kStatusStackOverflow;
     }
@@ -263,6 +273,7 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
     const uint32_t meta = ((k < 4 ? m0 : m1) >> (8 * (k & 3))) & 0xFFu;
     const uint32_t first = prim_base + (meta & 31u), n = meta >> 5;
     for (uint32_t j = 0; j < n; ++j) {
+      if (kCount) ++cnt->tris;
       const float4* tp = s.tris + 3 * (size_t)(first + j);
       const float4 a = ld4(tp), b = ld4(tp + 1), c = ld4(tp + 2);
       const V3 e1 = xyz(b), e2 = xyz(c);
@@ -292,12 +303,13 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
 }
 
 // Closest (or any) hit of one world-space ray.  Returns the status bits it raised.
-template <bool kAny>
-__device__ __forceinline__ uint32_t trace_ray(const DevScene& s, const V3 wo, const V3 wd, Hit& h) {
+template <bool kAny, bool kCount = false>
+__device__ __forceinline__ uint32_t trace_ray(const DevScene& s, const V3 wo, const V3 wd, Hit& h,
+                                              TraceCount* cnt = nullptr) {
   TraceState t;
   uint2 stack[kStackSize + 2];
   trace_begin(t, stack, s, wo, wd);
-  while (trace_step<kAny>(t, stack, s)) {
+  while (trace_step<kAny, kCount>(t, stack, s, cnt)) {
   }
   const uint2 uv = stack[kHitSlot], ti = stack[kHitSlot + 1];
   h.t = t.t_hit;
@@ -456,9 +468,12 @@ __global__ void __launch_bounds__(256) k_raygen(PathBatch pb, const WaveTables w
 // one small patch of the image with one direction bin (later bounces), so the lanes of a warp
 // walk largely the same nodes (shared cache lines, agreeing branches).  Refilling finished lanes one by one with
 // unrelated rays, with or without a warp-wide sync per node step, measured 11-30% slower.
-template <bool kSingle>
+// kCount: the instrumented variant, which also adds the TraceCount totals of the launch to
+// counters[8 * bounce + 0..4] (run only when a caller asks for the counters).
+template <bool kSingle, bool kCount>
 __global__ void __launch_bounds__(128, 7) k_trace_wave(PathBatch pb, const WaveTables wt, uint32_t bounce,
-                                                       unsigned long long* __restrict__ ray_total) {
+                                                       unsigned long long* __restrict__ ray_total,
+                                                       unsigned long long* __restrict__ counters) {
   __shared__ DevScene scenes[kSingle ? 1 : nb::kMaxWaveScenes];
   if (!kSingle) {
     for (uint32_t i = threadIdx.x; i < wt.n_scenes; i += blockDim.x) scenes[i] = wt.scenes[i];
@@ -469,6 +484,7 @@ __global__ void __launch_bounds__(128, 7) k_trace_wave(PathBatch pb, const WaveT
   const float4* __restrict__ qd = (bounce & 1) ? pb.q_d[1] : pb.q_d[0];
   const int lane = threadIdx.x & 31;
   uint32_t st = 0;
+  TraceCount cnt;
   while (true) {
     uint32_t base = 0;
     if (lane == 0) base = atomicAdd(pb.fetch + bounce, 32u);
@@ -478,12 +494,23 @@ __global__ void __launch_bounds__(128, 7) k_trace_wave(PathBatch pb, const WaveT
     if (i < n) {
       const float4 o = qo[i], d = qd[i];
       Hit h;
-      st |= trace_ray<false>(kSingle ? wt.scenes[0] : scenes[__float_as_uint(d.w)], xyz(o), xyz(d), h);
+      st |= trace_ray<false, kCount>(kSingle ? wt.scenes[0] : scenes[__float_as_uint(d.w)], xyz(o), xyz(d), h,
+                                     &cnt);
       pb.hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
       pb.hit_inst[i] = h.inst;
     }
   }
   if (st) atomicOr(pb.status, st);
+  if (kCount) {
+    const uint32_t c[5] = {cnt.tlas_nodes, cnt.blas_nodes, cnt.tris, cnt.insts, cnt.pushes};
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      unsigned long long v = c[k];
+      for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
+      if (lane == 0 && v) atomicAdd(counters + 8 * bounce + k, v);
+    }
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + 8 * bounce + 5, (unsigned long long)n);
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(ray_total, (unsigned long long)n);
 }
 
@@ -1398,13 +1425,22 @@ cudaError_t launch_raygen(const PathBatch& pb, const WaveTables& wt, int sms, cu
 }
 
 cudaError_t launch_trace_wave(const PathBatch& pb, const WaveTables& wt, bool single_scene, uint32_t bounce,
-                              unsigned long long* ray_total, int sms, cudaStream_t st) {
-  if (single_scene) {
-    static const int g = blocks_for((const void*)nbd::k_trace_wave<true>, 128, sms);
-    nbd::k_trace_wave<true><<<g, 128, 0, st>>>(pb, wt, bounce, ray_total);
+                              unsigned long long* ray_total, int sms, cudaStream_t st,
+                              unsigned long long* counters) {
+  if (counters) {
+    if (single_scene) {
+      static const int g = blocks_for((const void*)nbd::k_trace_wave<true, true>, 128, sms);
+      nbd::k_trace_wave<true, true><<<g, 128, 0, st>>>(pb, wt, bounce, ray_total, counters);
+    } else {
+      static const int g = blocks_for((const void*)nbd::k_trace_wave<false, true>, 128, sms);
+      nbd::k_trace_wave<false, true><<<g, 128, 0, st>>>(pb, wt, bounce, ray_total, counters);
+    }
+  } else if (single_scene) {
+    static const int g = blocks_for((const void*)nbd::k_trace_wave<true, false>, 128, sms);
+    nbd::k_trace_wave<true, false><<<g, 128, 0, st>>>(pb, wt, bounce, ray_total, nullptr);
   } else {
-    static const int g = blocks_for((const void*)nbd::k_trace_wave<false>, 128, sms);
-    nbd::k_trace_wave<false><<<g, 128, 0, st>>>(pb, wt, bounce, ray_total);
+    static const int g = blocks_for((const void*)nbd::k_trace_wave<false, false>, 128, sms);
+    nbd::k_trace_wave<false, false><<<g, 128, 0, st>>>(pb, wt, bounce, ray_total, nullptr);
   }
   return cudaGetLastError();
 }

@@ -67,9 +67,13 @@ cudaError_t launch_trace_rays(const nbd::DevScene& s, const float* rays, uint32_
                               uint32_t* inst, uint32_t* fetch, uint32_t* status, int sms, cudaStream_t st);
 
 cudaError_t launch_raygen(const PathBatch& pb, const WaveTables& wt, int sms, cudaStream_t st);
-// single_scene: all paths use wt.scenes[0] (passed by value); otherwise each ray's scene index
+// single_scene: all paths use wt.scenes[0] (passed by value); otherwise each ray's scene index.
+// counters (optional): runs the instrumented traversal, which adds its work counters (TLAS
+// node tests, BLAS node tests, triangle tests, instance entries, stack pushes) to
+// counters[8 * bounce + 0..4].
 cudaError_t launch_trace_wave(const PathBatch& pb, const WaveTables& wt, bool single_scene, uint32_t bounce,
-                              unsigned long long* ray_total, int sms, cudaStream_t st);
+                              unsigned long long* ray_total, int sms, cudaStream_t st,
+                              unsigned long long* counters = nullptr);
 cudaError_t launch_shade(const PathBatch& pb, const WaveTables& wt, uint32_t bounce, int sms, cudaStream_t st);
 // Shadow rays of environment next-event estimation: one per path and bounce at most.
 struct ShadowQueue {

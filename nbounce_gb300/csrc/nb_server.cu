@@ -21,6 +21,13 @@
 // wave packs the pending cache jobs of one scene like an ordinary wave packs the others.  When
 // both kinds are pending the scheduler alternates between a cache wave and an ordinary one.
 // The caches' buffers are outside the HBM budget's accounting.
+//
+// Failure handling, all on the host side of the GPU work: a bounded queue sheds load beyond
+// saturation (submit returns NB_ERR_BUSY), a job can be cancelled or given a deadline (it
+// finishes with NB_ERR_CANCELLED / NB_ERR_EXPIRED; waves of it already on the GPU run to
+// completion and its image is freed after them, stream-ordered), and a failed image
+// allocation fails only its job (NB_ERR_OOM).  A job record stays alive while a wave on the
+// GPU still refers to it, even if the caller releases it.
 
 #include <algorithm>
 #include <chrono>
@@ -50,6 +57,8 @@ struct Job {
   uint32_t next_sample = 1;  // next Sobol row to plan
   uint32_t planned_waves = 0, finished_waves = 0;
   bool fully_planned = false;
+  bool released = false;     // the caller released it; erased once no wave refers to it
+  uint32_t inflight_refs = 0;  // waves on the GPU with a segment of this job
   float* d_img = nullptr;
   size_t bytes = 0;
   double t_submit = 0, t_admit = 0, t_finish = 0;
@@ -98,8 +107,13 @@ struct nb_server {
   std::vector<cudaEvent_t> event_pool;
   Clock::time_point t0 = Clock::now();
 
+  uint32_t queue_limit = 0;       // 0: unbounded
+  uint32_t fail_alloc_in = 0;     // the fail_alloc_in-th image allocation from now fails (0: off)
+  bool has_deadlines = false;
+
   // statistics (guarded by mu)
   uint64_t jobs_submitted = 0, jobs_done = 0, jobs_failed = 0, waves = 0;
+  uint64_t jobs_rejected = 0, jobs_cancelled = 0, jobs_expired = 0;
   double gpu_busy_ms = 0.0;
   uint64_t bytes_in_use = 0, peak_bytes = 0;
 
@@ -137,8 +151,13 @@ struct nb_server {
   template <class Pick>
   void fail_jobs_locked(Pick pick, int status) {
     auto doomed = [&](Job* j) { return j->state != Job::kDone && pick(j); };
+    auto count = [&] {
+      ++jobs_failed;
+      if (status == NB_ERR_CANCELLED) ++jobs_cancelled;
+      if (status == NB_ERR_EXPIRED) ++jobs_expired;
+    };
     for (Job* j : queue)
-      if (doomed(j)) j->state = Job::kDone, j->status = status, j->t_finish = now_ms(), ++jobs_failed;
+      if (doomed(j)) j->state = Job::kDone, j->status = status, j->t_finish = now_ms(), count();
     queue.erase(std::remove_if(queue.begin(), queue.end(), [](Job* j) { return j->state == Job::kDone; }),
                 queue.end());
     for (Job* j : active) {
@@ -151,11 +170,25 @@ struct nb_server {
       j->state = Job::kDone;
       j->status = status;
       j->t_finish = now_ms();
-      ++jobs_failed;
+      count();
     }
     active.erase(std::remove_if(active.begin(), active.end(), [](Job* j) { return j->state == Job::kDone; }),
                  active.end());
     cv_done.notify_all();
+  }
+
+  // fails the queued and active jobs whose deadline has passed
+  void expire_locked() {
+    if (!has_deadlines) return;
+    const double now = now_ms();
+    fail_jobs_locked([now](const Job* j) { return j->desc.deadline_ms && now > j->t_submit + j->desc.deadline_ms; },
+                     NB_ERR_EXPIRED);
+  }
+
+  // drops a wave's reference to a job; a released job is erased with its last reference
+  void unref_locked(Job* j) {
+    if (j->inflight_refs) --j->inflight_refs;
+    if (j->released && j->inflight_refs == 0) jobs.erase(j->id);
   }
 
   void admit_locked() {
@@ -164,7 +197,9 @@ struct nb_server {
       if (bytes_in_use + j->bytes > budget) break;  // wait for images to be delivered
       queue.pop_front();
       void* p = nullptr;
-      cudaError_t e = cudaMallocAsync(&p, j->bytes, stream);
+      cudaError_t e;
+      if (fail_alloc_in && --fail_alloc_in == 0) e = cudaErrorMemoryAllocation;  // nb_server_fail_alloc
+      else e = cudaMallocAsync(&p, j->bytes, stream);
       if (e == cudaSuccess) e = cudaMemsetAsync(p, 0, j->bytes, stream);
       if (e != cudaSuccess) {
         j->state = Job::kDone;
@@ -246,6 +281,7 @@ struct nb_server {
       j->next_sample += want[i];
       j->fully_planned = j->next_sample > j->desc.spp;
       j->planned_waves += 1;
+      j->inflight_refs += 1;
       *max_bounces = std::max(*max_bounces, j->desc.bounces);
       wave_jobs->push_back(j);
     }
@@ -346,6 +382,7 @@ struct nb_server {
     cudaSetDevice(device);
     std::unique_lock<std::mutex> lk(mu);
     for (;;) {
+      expire_locked();
       admit_locked();
       bool launched = false;
       if (inflight.size() < 2) {
@@ -369,6 +406,7 @@ struct nb_server {
             CacheWave cw{};
             const int setup = prepare_cache_wave(cache_scene, &c, &cw);
             if (setup != NB_OK) {  // the scene's cache jobs fail; the other jobs go on
+              for (Job* j : w.jobs) unref_locked(j);
               fail_jobs_locked([&](const Job* j) { return (j->desc.flags & NB_JOB_CACHE) && j->desc.scene == cache_scene; },
                                setup);
               event_pool.push_back(w.start);
@@ -408,9 +446,11 @@ struct nb_server {
         }
         gpu_busy_ms += ms;
         for (Job* j : w.jobs) {
-          if (j->state == Job::kDone) continue;  // failed while this wave ran
-          j->finished_waves += 1;
-          if (j->fully_planned && j->finished_waves == j->planned_waves) complete_locked(j);
+          if (j->state != Job::kDone) {  // else it failed while this wave ran
+            j->finished_waves += 1;
+            if (j->fully_planned && j->finished_waves == j->planned_waves) complete_locked(j);
+          }
+          unref_locked(j);
         }
         event_pool.push_back(w.start);
         event_pool.push_back(w.stop);
@@ -535,6 +575,10 @@ int nb_server_submit(nb_server* s, const nb_job_desc* desc, uint64_t* job_id) {
   if (desc->scene >= s->scenes.size() || desc->env >= s->envs.size())
     return fail(NB_ERR_INVALID_ARG, "unknown scene or environment slot");
   if (s->stopping) return fail(NB_ERR_INVALID_ARG, "server is shutting down");
+  if (s->queue_limit && s->queue.size() >= s->queue_limit) {
+    ++s->jobs_rejected;
+    return fail(NB_ERR_BUSY, "queue full (%u jobs waiting for admission)", s->queue_limit);
+  }
   std::unique_ptr<Job> j(new (std::nothrow) Job());
   if (!j) return fail(NB_ERR_OOM, "host allocation failed");
   j->desc = *desc;
@@ -542,6 +586,7 @@ int nb_server_submit(nb_server* s, const nb_job_desc* desc, uint64_t* job_id) {
   if (s->fixed_bytes + j->bytes > s->budget) return fail(NB_ERR_OOM, "job image does not fit the budget");
   j->id = s->next_id++;
   j->t_submit = s->now_ms();
+  if (desc->deadline_ms) s->has_deadlines = true;
   s->queue.push_back(j.get());
   *job_id = j->id;
   s->jobs.emplace(j->id, std::move(j));
@@ -554,7 +599,8 @@ int nb_server_wait(nb_server* s, uint64_t job_id, int timeout_ms, nb_job_info* i
   if (!s) return fail(NB_ERR_INVALID_ARG, "NULL argument");
   std::unique_lock<std::mutex> lk(s->mu);
   auto it = s->jobs.find(job_id);
-  if (it == s->jobs.end()) return fail(NB_ERR_INVALID_ARG, "unknown job %llu", (unsigned long long)job_id);
+  if (it == s->jobs.end() || it->second->released)
+    return fail(NB_ERR_INVALID_ARG, "unknown job %llu", (unsigned long long)job_id);
   Job* j = it->second.get();
   auto done = [&] { return j->state == Job::kDone; };
   if (timeout_ms < 0) s->cv_done.wait(lk, done);
@@ -574,7 +620,7 @@ int nb_server_fetch(nb_server* s, uint64_t job_id, float* host_rgba) {
   if (!s || !host_rgba) return fail(NB_ERR_INVALID_ARG, "NULL argument");
   std::lock_guard<std::mutex> lk(s->mu);
   auto it = s->jobs.find(job_id);
-  if (it == s->jobs.end()) return fail(NB_ERR_INVALID_ARG, "unknown job");
+  if (it == s->jobs.end() || it->second->released) return fail(NB_ERR_INVALID_ARG, "unknown job");
   Job* j = it->second.get();
   if (j->state != Job::kDone) return fail(NB_ERR_TIMEOUT, "job not finished");
   if (j->status != NB_OK) return fail(j->status, "job failed");
@@ -592,14 +638,44 @@ int nb_server_release(nb_server* s, uint64_t job_id) {
   if (!s) return fail(NB_ERR_INVALID_ARG, "NULL argument");
   std::lock_guard<std::mutex> lk(s->mu);
   auto it = s->jobs.find(job_id);
-  if (it == s->jobs.end()) return fail(NB_ERR_INVALID_ARG, "unknown job");
+  if (it == s->jobs.end() || it->second->released) return fail(NB_ERR_INVALID_ARG, "unknown job");
   Job* j = it->second.get();
   if (j->state != Job::kDone) return fail(NB_ERR_INVALID_ARG, "job not finished");
   if (j->d_img) {
     cudaFreeAsync(j->d_img, s->stream);
+    j->d_img = nullptr;
     s->bytes_in_use -= j->bytes;
+    s->cv_work.notify_one();
   }
-  s->jobs.erase(it);
+  if (j->inflight_refs) j->released = true;  // a wave on the GPU still refers to it
+  else s->jobs.erase(it);
+  return NB_OK;
+}
+
+int nb_server_set_queue_limit(nb_server* s, uint32_t max_queued) {
+  if (!s) return fail(NB_ERR_INVALID_ARG, "NULL argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->queue_limit = max_queued;
+  return NB_OK;
+}
+
+int nb_server_cancel(nb_server* s, uint64_t job_id) {
+  if (!s) return fail(NB_ERR_INVALID_ARG, "NULL argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  auto it = s->jobs.find(job_id);
+  if (it == s->jobs.end() || it->second->released)
+    return fail(NB_ERR_INVALID_ARG, "unknown job %llu", (unsigned long long)job_id);
+  Job* j = it->second.get();
+  if (j->state == Job::kDone) return fail(NB_ERR_INVALID_ARG, "job %llu already finished", (unsigned long long)job_id);
+  s->fail_jobs_locked([j](const Job* x) { return x == j; }, NB_ERR_CANCELLED);
+  s->cv_work.notify_one();
+  return NB_OK;
+}
+
+int nb_server_fail_alloc(nb_server* s, uint32_t nth) {
+  if (!s) return fail(NB_ERR_INVALID_ARG, "NULL argument");
+  std::lock_guard<std::mutex> lk(s->mu);
+  s->fail_alloc_in = nth;
   return NB_OK;
 }
 
@@ -620,6 +696,11 @@ int nb_server_get_stats(nb_server* s, nb_server_stats* out) {
   out->budget_bytes = s->budget;
   out->queued = (uint32_t)s->queue.size();
   out->active = (uint32_t)s->active.size();
+  out->jobs_rejected = s->jobs_rejected;
+  out->jobs_cancelled = s->jobs_cancelled;
+  out->jobs_expired = s->jobs_expired;
+  out->queue_limit = s->queue_limit;
+  out->reserved = 0;
   return NB_OK;
 }
 

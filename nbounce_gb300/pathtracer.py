@@ -321,6 +321,18 @@ class Pathtracer:
         check(lib().nb_pathtracer_kernel_times(self._h, C.byref(t), int(reset), _stream(stream)))
         return {k: getattr(t, k) for k, _ in L.NbKernelTimes._fields_}
 
+    def enable_trace_counters(self, enable=True):
+        """Runs the instrumented traversal (same images, slower) that counts per bounce the
+        wide nodes, triangles and instances it fetches and the stack entries it pushes."""
+        check(lib().nb_pathtracer_enable_trace_counters(self._h, int(enable)))
+
+    def trace_counters(self, n_bounces, reset=True, stream=None):
+        """[{rays, tlas_node_tests, blas_node_tests, triangle_tests, instance_entries,
+        stack_pushes}] for bounces 0 .. n_bounces - 1 since the last reset."""
+        arr = (L.NbTraceCounters * n_bounces)()
+        check(lib().nb_pathtracer_trace_counters(self._h, arr, int(n_bounces), int(reset), _stream(stream)))
+        return [{k: int(getattr(c, k)) for k, _ in L.NbTraceCounters._fields_} for c in arr]
+
     def close(self):
         if self._h:
             lib().nb_pathtracer_destroy(self._h)

@@ -1,14 +1,16 @@
 """Host logic for running the pass on several ranks (one process per GPU).
 
-Two modes, both without any collective inside the data path:
+Two modes:
 
 * replicas (what bench.py --gpus N runs): every rank renders its own frame; throughput is
-  the rays of all ranks over the slowest rank's time (``aggregate_replicas``).
-* sample sharding (one frame over N ranks): rank r sets its Pathtracer's sample counter to
+  the rays of all ranks over the slowest rank's time (``aggregate_replicas``); no collective.
+* sample sharding (one frame over N ranks, bench.py --shard-frame): rank r sets its
+  Pathtracer's sample counter to
   start - 1 and renders a contiguous range of Sobol rows (``shard_samples``).  Its running
   mean (mix with weight 1/k, pathtracing.wgsl:258) then holds sum(L) / last_row, so one
   exchange merges the ranks as sum_r(last_row_r * mean_r) / sum_r(count_r)
-  (``merge_running_means``).  The merge equals the single-rank running mean up to float
+  (``merge_running_means``; ``merge_running_means_distributed`` is the one all-reduce, on the
+  device for CUDA tensors).  The merge equals the single-rank running mean up to float
   rounding (not bit-exact: the reference's mean is a chain of mix() steps in sample order).
 """
 import numpy as np
@@ -35,10 +37,22 @@ def merge_running_means(means, last_rows, counts):
 
 
 def merge_running_means_distributed(mean, last_row, count, group=None):
-    """The exchange step across ranks: all-reduce of last_row * mean and of count."""
+    """The exchange step across ranks: all-reduce of last_row * mean and of count.
+
+    `mean` is a numpy array (reduced on the host: gloo) or a torch tensor, which is reduced
+    where it lives (a CUDA tensor stays on its GPU: NCCL) and returned as a float32 tensor
+    there; the numpy form returns numpy."""
     import torch
     import torch.distributed as dist
 
+    if isinstance(mean, torch.Tensor):
+        t = mean.to(torch.float64) * float(last_row)
+        n = torch.tensor([float(count)], dtype=torch.float64, device=mean.device)
+        dist.all_reduce(t, group=group)
+        dist.all_reduce(n, group=group)
+        out = (t / n).to(torch.float32)
+        out[..., 3] = 1.0
+        return out
     t = torch.as_tensor(np.asarray(mean, np.float64) * last_row)
     n = torch.tensor([float(count)], dtype=torch.float64)
     dist.all_reduce(t, group=group)

@@ -473,3 +473,32 @@ def incoherent_rays(n, seed=0x5EED3):
     d = rng.normal(size=(n, 3))
     out[:, 4:7] = d / np.linalg.norm(d, axis=1, keepdims=True)
     return out
+
+
+def stratified_tiles(width, height, nx=6, ny=4, size=16):
+    """nx * ny square tiles of `size` pixels, one centred in each cell of an nx x ny grid over
+    the frame: (x0, y0, size, size) row by row.  The relMSE truth images and the CPU timing
+    samples use these tiles, so that every part of the frame is weighted alike."""
+    out = []
+    for j in range(ny):
+        for i in range(nx):
+            x0 = (2 * i + 1) * width // (2 * nx) - size // 2
+            y0 = (2 * j + 1) * height // (2 * ny) - size // 2
+            out.append((int(x0), int(y0), int(size), int(size)))
+    return out
+
+
+def scene_fingerprint(desc):
+    """A few numbers that change whenever the seeded generator's output changes: triangle and
+    instance counts and binary64 sums of the vertex positions and instance transforms."""
+    pos = desc.vertices["pos"].astype(np.float64)
+    l2w = np.array([i["l2w"] for i in desc.instances], np.float64)
+    return {"triangles": int(desc.n_triangles_unique), "instances": len(desc.instances),
+            "pos_sum": float(pos.sum()), "l2w_sum": float(l2w.sum())}
+
+
+def cache_camera(width=1920, height=1080, n_frames=300):
+    """(world_to_clip, clip_to_world) of the radiance-cache workload's last camera: the end of
+    camera_path, which sits on the spline's last key whatever the frame count."""
+    eye, target = camera_path(n_frames)[-1]
+    return camera_matrices(eye, target, width, height)

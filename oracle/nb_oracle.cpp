@@ -1005,38 +1005,36 @@ static uint64_t render_region(const RenderArgs& a, uint32_t first_sample, uint32
                               uint32_t* overflow_flag, uint64_t* counters) {
   std::atomic<uint64_t> total_rays{0}, total_aabb{0}, total_tri{0}, total_inst{0};
   std::atomic<uint32_t> ovf{0};
-  uint32_t tiles_x = (w + 7) / 8, tiles_y = (h + 7) / 8;
-  parallel_for(tiles_x * tiles_y, threads, [&](uint32_t tile) {
-    uint32_t tx = tile % tiles_x, ty = tile / tiles_x;
+  // one work item per pixel (regions can be a few pixels wide; samples stay in order per pixel)
+  parallel_for(w * h, threads, [&](uint32_t item) {
     WorkCounters wc;
     bool overflow = false;
-    for (uint32_t yy = ty * 8; yy < std::min(h, ty * 8 + 8); ++yy) {
-      for (uint32_t xx = tx * 8; xx < std::min(w, tx * 8 + 8); ++xx) {
-        uint32_t px = x0 + xx, py = y0 + yy;
-        size_t o = (size_t)yy * w + xx;
-        uint32_t hin[4] = {px, py, px, py};
-        float shift[4];
-        hash4f(hin, shift);
-        float cr = out_rgba[4 * o], cg = out_rgba[4 * o + 1], cb = out_rgba[4 * o + 2];
-        for (uint32_t k = 0; k < spp; ++k) {
-          uint32_t sample = first_sample + k;
-          float weight = 1.0f / (float)sample;  // pathtracer.rs:235
-          Rand4<R> j = cp_rotate<R>(sobol_read(a.sobol, a.sobol_n, (uint64_t)sample * kLdsStride), shift);
-          Ray<R> ray = generate_ray<R>(px, py, a.W, a.H, j.x, j.y, a.c2w);
-          V3<R> L = sample_rendering_eq<R>(a, sample, shift, ray, &wc, &overflow);
-          float lr = (float)L.x, lg = (float)L.y, lb = (float)L.z;
-          if (per_sample) {
-            float* q = per_sample + 4 * (o * spp + k);
-            q[0] = lr; q[1] = lg; q[2] = lb; q[3] = 1.0f;
-          }
-          // mix(color, L, weight) (pathtracing.wgsl:258)
-          cr = cr * (1.0f - weight) + lr * weight;
-          cg = cg * (1.0f - weight) + lg * weight;
-          cb = cb * (1.0f - weight) + lb * weight;
-        }
-        out_rgba[4 * o] = cr; out_rgba[4 * o + 1] = cg; out_rgba[4 * o + 2] = cb; out_rgba[4 * o + 3] = 1.0f;
+    const uint32_t xx = item % w, yy = item / w;
+    const uint32_t px = x0 + xx, py = y0 + yy;
+    const size_t o = (size_t)yy * w + xx;
+    uint32_t hin[4] = {px, py, px, py};
+    float shift[4];
+    hash4f(hin, shift);
+    // the running mean is kept in R: binary32 is the reference's own mix (pathtracing.wgsl:258);
+    // the binary64 truth mode averages its binary64 samples in binary64
+    R cr = out_rgba[4 * o], cg = out_rgba[4 * o + 1], cb = out_rgba[4 * o + 2];
+    for (uint32_t k = 0; k < spp; ++k) {
+      uint32_t sample = first_sample + k;
+      R weight = R(1) / (R)sample;  // pathtracer.rs:235
+      Rand4<R> j = cp_rotate<R>(sobol_read(a.sobol, a.sobol_n, (uint64_t)sample * kLdsStride), shift);
+      Ray<R> ray = generate_ray<R>(px, py, a.W, a.H, j.x, j.y, a.c2w);
+      V3<R> L = sample_rendering_eq<R>(a, sample, shift, ray, &wc, &overflow);
+      if (per_sample) {
+        float* q = per_sample + 4 * (o * spp + k);
+        q[0] = (float)L.x; q[1] = (float)L.y; q[2] = (float)L.z; q[3] = 1.0f;
       }
+      // mix(color, L, weight) (pathtracing.wgsl:258)
+      cr = cr * (R(1) - weight) + L.x * weight;
+      cg = cg * (R(1) - weight) + L.y * weight;
+      cb = cb * (R(1) - weight) + L.z * weight;
     }
+    out_rgba[4 * o] = (float)cr; out_rgba[4 * o + 1] = (float)cg; out_rgba[4 * o + 2] = (float)cb;
+    out_rgba[4 * o + 3] = 1.0f;
     total_rays += wc.rays;
     total_aabb += wc.n_aabb;
     total_tri += wc.n_tri;

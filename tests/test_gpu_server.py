@@ -191,9 +191,8 @@ def test_rejected_cache_config_fails_only_the_cache_jobs(world):
         ids.append(srv.submit(slots[k], env_slots[k], w2c, c2w, w, h, spp, b, out=out, flags=f))
     for jid, (k, w, h, spp, b), out, f in zip(ids, JOBS, outs, flags):
         if f:
-            with pytest.raises(nb.NbError) as e:
-                srv.wait(jid, timeout_ms=120000)
-            assert e.value.status == 1
+            info = srv.wait(jid, timeout_ms=120000)
+            assert info["done"] == 1 and info["status"] == 1
         else:
             info = srv.wait(jid, timeout_ms=120000)
             assert info["done"] == 1 and info["status"] == 0
@@ -274,5 +273,86 @@ def test_burst_of_small_jobs_completes_and_frees_its_memory(world):
     st = srv.stats()
     assert st["jobs_done"] == 400 and st["jobs_failed"] == 0
     assert st["peak_bytes_in_use"] <= budget
+    assert st["bytes_in_use"] == idle
+    srv.close()
+
+
+def test_cancelled_expired_and_out_of_memory_jobs_fail_alone(world):
+    """Host-side failure cases (no GPU fault is involved): a job whose image allocation fails
+    (nb_server_fail_alloc arms the second allocation to fail as cudaMallocAsync does when
+    memory runs out), a job cancelled while it waits in the queue, a job cancelled after some
+    of its waves ran, and a job whose deadline passes.  Each finishes with its own status; the
+    other jobs' images equal the same jobs rendered alone; once every job is released the
+    server holds only its fixed buffers again."""
+    import time
+    paths = 1 << 12
+    budget = fixed_bytes(paths) + 64 * 64 * 16 + 4 * 32 * 32 * 16  # one 64x64 image at a time
+    srv = RenderServer(hbm_budget_bytes=budget, paths_per_wave=paths)
+    slots = [srv.add_scene(s) for s in world["scenes"]]
+    env_slots = [srv.add_env(e) for e in world["envs"]]
+    idle = srv.stats()["bytes_in_use"]
+    srv.fail_alloc(2)
+    jobs = {"a": (0, 32, 32, 3, 6, 0), "oom": (1, 32, 32, 2, 8, 0), "big": (0, 64, 64, 1000, 6, 0),
+            "queued": (1, 64, 64, 4, 8, 0), "late": (0, 24, 24, 1000, 6, 1), "f": (1, 40, 24, 2, 8, 0)}
+    ids, outs = {}, {}
+    for name, (k, w, h, spp, b, deadline) in jobs.items():
+        w2c, c2w = scenes.camera_matrices(*CAMS[k], w, h)
+        outs[name] = np.full((h, w, 4), np.nan, np.float32)
+        ids[name] = srv.submit(slots[k], env_slots[k], w2c, c2w, w, h, spp, b, out=outs[name],
+                               deadline_ms=deadline)
+        if name == "queued":  # waits behind "big"'s image for budget
+            srv.cancel(ids[name])
+    t0 = time.time()
+    while srv.stats()["waves"] < 3 and time.time() - t0 < 60:
+        time.sleep(0.001)
+    srv.cancel(ids["big"])
+    infos = {n: srv.wait(j, timeout_ms=120000) for n, j in ids.items()}
+    assert all(i["done"] == 1 for i in infos.values())
+    want = {"a": 0, "oom": L.NB_ERR_OOM, "big": L.NB_ERR_CANCELLED, "queued": L.NB_ERR_CANCELLED,
+            "late": L.NB_ERR_EXPIRED, "f": 0}
+    assert {n: i["status"] for n, i in infos.items()} == want
+    for name in ("a", "f"):
+        k, w, h, spp, b, _ = jobs[name]
+        assert np.array_equal(outs[name], alone(world, k, w, h, spp, b)), name
+    with pytest.raises(nb.NbError) as e:  # a finished job cannot be cancelled
+        srv.cancel(ids["a"])
+    assert e.value.status == L.NB_ERR_INVALID_ARG
+    st = srv.stats()
+    assert (st["jobs_cancelled"], st["jobs_expired"], st["jobs_failed"], st["jobs_done"]) == (2, 1, 4, 2)
+    for j in ids.values():
+        srv.release(j)
+    assert srv.stats()["bytes_in_use"] == idle
+    srv.close()  # waits for the cancelled jobs' waves still on the GPU
+
+
+def test_overload_sheds_jobs_and_returns_to_idle(world):
+    """Two hundred jobs submitted back to back against a queue limit of 8: submissions beyond
+    the limit are rejected with NB_ERR_BUSY at once, every admitted job completes (no stall),
+    and after the jobs are released the server's device memory is back to its idle level."""
+    paths = 1 << 14
+    srv = RenderServer(hbm_budget_bytes=1 << 30, paths_per_wave=paths)
+    slots = [srv.add_scene(s) for s in world["scenes"]]
+    env_slots = [srv.add_env(e) for e in world["envs"]]
+    srv.set_queue_limit(8)
+    idle = srv.stats()["bytes_in_use"]
+    rng = np.random.default_rng(5)
+    accepted, rejected = [], 0
+    for n in range(200):
+        k = int(rng.integers(2))
+        w, h = int(rng.integers(16, 65)), int(rng.integers(16, 65))
+        w2c, c2w = scenes.camera_matrices(*CAMS[k], w, h)
+        jid = srv.submit(slots[k], env_slots[k], w2c, c2w, w, h, int(rng.integers(1, 9)), 8, busy_ok=True)
+        if jid is None:
+            rejected += 1
+        else:
+            accepted.append(jid)
+    assert rejected > 0 and len(accepted) >= 8
+    for jid in accepted:
+        info = srv.wait(jid, timeout_ms=120000)
+        assert info["done"] == 1 and info["status"] == 0
+        srv.release(jid)
+    st = srv.stats()
+    assert st["jobs_rejected"] == rejected and st["jobs_submitted"] == len(accepted)
+    assert st["jobs_done"] == len(accepted) and st["queued"] == 0 and st["active"] == 0
     assert st["bytes_in_use"] == idle
     srv.close()

@@ -1,0 +1,144 @@
+"""Parity at the benchmark workloads' own sizes.
+
+* 64-icosphere workload at its stated size (256 x 256, 16 spp, 6 bounces, constant sky): the
+  GPU image against the oracle's binary32 render of the same samples (>= 99% of pixels
+  bit-equal, relMSE <= 1e-4), and the GPU render of the binary64 truth's own 16,384 samples
+  against that truth (tests/golden/truth_spheres_256.npz): the binary32 pass and the binary64
+  restatement may part only where rounding sends a path another way, which averages out over
+  the samples (relMSE <= 1e-5; the oracle's own binary32 render at 256 spp is 1.0e-5 from
+  its binary64 render, and the gap falls as 1/spp).
+* 1M-triangle soup (the traversal workload: 16,777,216 rays, coherent 1024 x 16384 pinhole
+  grid and uniform incoherent rays): a 262,144-ray slice of each set (every 64th coherent
+  ray, the first 262,144 incoherent ones) traced by the GPU and the oracle; closest hits with
+  the traversal bars (ids exact except near-ties, t/u/v within 1e-5 relative), any-hit with
+  the same occlusion answer and t no closer than the closest hit.
+"""
+import numpy as np
+import pytest
+
+import nbounce_gb300 as nb
+from nbounce_gb300 import scenes
+from oracle import oracle as O
+
+from test_gpu_render import EXACT_FRAC, REL_MSE, rel_mse
+from test_gpu_trace import NO_HIT, compare_hits
+
+pytestmark = pytest.mark.gpu
+
+TRUTH_REL_MSE = 1e-5
+
+
+def _load_truth(name):
+    import os
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", f"truth_{name}.npz")
+    d = np.load(path)
+    return {k: d[k] for k in d.files}
+
+
+@pytest.fixture(scope="module")
+def spheres_c0():
+    desc = scenes.spheres_scene(width=256, height=256, spp=16, bounces=6)
+    scene = nb.SceneBuffers.from_desc(desc)
+    env = nb.EnvMap(desc.env_color)
+    cam = nb.camera_struct(desc.world_to_clip, desc.clip_to_world)
+    return desc, scene, env, cam
+
+
+def test_spheres_workload_full_size_matches_oracle(spheres_c0):
+    desc, scene, env, cam = spheres_c0
+    pt = nb.Pathtracer(256, 256, nb.Globals(bounces=6))
+    pt.render(scene, cam, env, 16)
+    img = pt.download()
+    rays, status = pt.last_stats()
+    assert status == 0
+    orc = O.OracleScene(desc.vertices, desc.indices, desc.primitives(), dedup=True)
+    ref, ref_rays, _, ovf = orc.render(desc.clip_to_world, 256, 256, O.sobol_table(), 1, 16, bounces=6,
+                                       env=desc.env_color)
+    assert not ovf
+    exact = float(np.mean(np.all(img == ref, axis=-1)))
+    assert exact >= EXACT_FRAC, exact
+    assert rel_mse(img, ref) <= REL_MSE
+    assert abs(rays - ref_rays) <= 0.001 * ref_rays
+
+
+def test_spheres_workload_truth_samples_match_binary64_truth(spheres_c0):
+    desc, scene, env, cam = spheres_c0
+    truth = _load_truth("spheres_256")
+    fp = scenes.scene_fingerprint(desc)
+    assert int(truth["fingerprint"][0]) == fp["triangles"] and int(truth["fingerprint"][1]) == fp["instances"]
+    spp = int(truth["spp"])
+    pt = nb.Pathtracer(256, 256, nb.Globals(bounces=6), sobol_table=nb.sobol_burley_table(spp, 17))
+    pt.render(scene, cam, env, spp)
+    img = pt.download()
+    assert pt.last_stats()[1] == 0
+    t = truth["rgb"][0]
+    assert img.shape[:2] == t.shape[:2]
+    assert rel_mse(img, t) <= TRUTH_REL_MSE, rel_mse(img, t)
+    # and 16 spp sits at the noise level the oracle's own 16 samples reach against the truth
+    pt16 = nb.Pathtracer(256, 256, nb.Globals(bounces=6))
+    pt16.render(scene, cam, env, 16)
+    orc = O.OracleScene(desc.vertices, desc.indices, desc.primitives(), dedup=True)
+    ref16, _, _, _ = orc.render(desc.clip_to_world, 256, 256, O.sobol_table(), 1, 16, bounces=6, env=desc.env_color)
+    g, c = rel_mse(pt16.download(), t), rel_mse(ref16, t)
+    assert abs(g - c) <= 0.01 * c, (g, c)
+
+
+@pytest.fixture(scope="module")
+def soup_1m():
+    desc = scenes.soup_scene(1 << 20)
+    gpu = nb.SceneBuffers.from_desc(desc, dedup=True)
+    orc = O.OracleScene(desc.vertices, desc.indices, desc.primitives(), dedup=True)
+    coherent = scenes.coherent_rays(1024, 16384)[::64]
+    incoherent = scenes.incoherent_rays(1 << 24, seed=0x5EED3)[:1 << 18]
+    return gpu, orc, {"coherent": np.ascontiguousarray(coherent), "incoherent": incoherent}
+
+
+@pytest.mark.parametrize("kind", ["coherent", "incoherent"])
+def test_soup_1m_closest_hit_matches_oracle(soup_1m, kind):
+    gpu, orc, rays = soup_1m
+    r = rays[kind]
+    assert r.shape[0] == 1 << 18
+    hits, inst = gpu.trace_host(r)
+    rf, ru, cnt = orc.trace(r)
+    assert cnt[:, 3].max() == 0
+    ties, both = compare_hits(hits, inst, gpu.export()["indices"], rf, ru)
+    assert both > 100000
+
+
+@pytest.mark.parametrize("kind", ["coherent", "incoherent"])
+def test_soup_1m_any_hit_matches_oracle(soup_1m, kind):
+    gpu, orc, rays = soup_1m
+    r = rays[kind]
+    any_hits, _ = gpu.trace_host(r, any_hit=True)
+    closest, _ = gpu.trace_host(r)
+    rf, _, _ = orc.trace(r, any_hit=True)
+    g_occ = any_hits[:, 0] != NO_HIT
+    assert np.array_equal(g_occ, closest[:, 0] != NO_HIT)
+    assert np.array_equal(g_occ, rf[:, 0] != NO_HIT)
+    assert np.all(any_hits[g_occ, 0] >= closest[g_occ, 0])
+    # an any-hit answer is a hit on a real triangle along the ray: t within the oracle's
+    # closest-hit bound from below and finite
+    assert np.all(np.isfinite(any_hits[g_occ, 0]))
+
+
+def test_trace_counters_leave_the_image_unchanged(spheres_c0):
+    """The instrumented traversal (nb_pathtracer_enable_trace_counters) renders the same image
+    and counts at least one node test and one ray per traced bounce."""
+    desc, scene, env, cam = spheres_c0
+    pt = nb.Pathtracer(256, 256, nb.Globals(bounces=6))
+    pt.render(scene, cam, env, 4)
+    plain = pt.download()
+    rays, _ = pt.last_stats()
+    pt.invalidate()
+    pt.enable_trace_counters(True)
+    pt.render(scene, cam, env, 4)
+    counted = pt.download()
+    c = pt.trace_counters(7)
+    assert np.array_equal(plain, counted)
+    assert sum(x["rays"] for x in c) == rays
+    assert c[0]["rays"] == 256 * 256 * 4
+    assert all(x["tlas_node_tests"] >= x["rays"] for x in c if x["rays"])
+    assert c[0]["triangle_tests"] > 0 and c[0]["instance_entries"] > 0
+    pt.enable_trace_counters(False)
+    with pytest.raises(nb.NbError):
+        pt.trace_counters(7)
