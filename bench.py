@@ -579,21 +579,27 @@ def configs_report(args):
         hits = torch.empty((n, 4), dtype=torch.float32, device="cuda")
         inst = torch.empty(n, dtype=torch.int32, device="cuda")
         for any_hit in (False, True):
-            for _ in range(3):
-                soup.trace_device(d_rays.data_ptr(), n, hits.data_ptr(), inst.data_ptr(), any_hit=any_hit)
-            a.record()
-            for _ in range(5):
-                soup.trace_device(d_rays.data_ptr(), n, hits.data_ptr(), inst.data_ptr(), any_hit=any_hit)
-            b.record()
-            b.synchronize()
-            gms = a.elapsed_time(b) / 5
+            gms = {}
+            for incoherent in (False, True):  # warps of 32 neighbours vs lane refill (NB_TRACE_INCOHERENT)
+                for _ in range(3):
+                    soup.trace_device(d_rays.data_ptr(), n, hits.data_ptr(), inst.data_ptr(), any_hit=any_hit,
+                                      incoherent=incoherent)
+                a.record()
+                for _ in range(5):
+                    soup.trace_device(d_rays.data_ptr(), n, hits.data_ptr(), inst.data_ptr(), any_hit=any_hit,
+                                      incoherent=incoherent)
+                b.record()
+                b.synchronize()
+                gms[incoherent] = a.elapsed_time(b) / 5
             m = 1 << 18
             t = time.perf_counter()
             osc.trace(rays[:m], any_hit=any_hit, threads=threads)
             cs = time.perf_counter() - t
+            best = min(gms.values())
             res[f"{kind}_{'any' if any_hit else 'closest'}"] = {
-                "gpu_mrays_s": round(n / gms / 1e3, 1), "gpu_ms": round(gms, 3), "cpu_mrays_s": round(m / cs / 1e6, 2),
-                "ratio": round((n / gms / 1e3) / (m / cs / 1e6), 1)}
+                "gpu_mrays_s": round(n / best / 1e3, 1), "gpu_ms": round(best, 3),
+                "gpu_ms_warp_of_neighbours": round(gms[False], 3), "gpu_ms_lane_refill": round(gms[True], 3),
+                "cpu_mrays_s": round(m / cs / 1e6, 2), "ratio": round((n / best / 1e3) / (m / cs / 1e6), 1)}
         del d_rays, hits, inst
     out["soup_1m_16m_rays"] = res
     return out

@@ -315,7 +315,11 @@ int nb_env_sample(const nb_env* env, const float* u, size_t n, float* out, void*
  * ------------------------------------------------------------------------------------- */
 enum {
   NB_TRACE_CLOSEST = 0,
-  NB_TRACE_ANY = 1u << 0 /* stop at the first accepted triangle (occlusion query) */
+  NB_TRACE_ANY = 1u << 0,       /* stop at the first accepted triangle (occlusion query) */
+  NB_TRACE_INCOHERENT = 1u << 1 /* neighbouring rays of the array are unrelated (scattered origins or
+                                   directions): a warp's lanes take new rays as theirs finish instead
+                                   of tracing 32 neighbours to the end.  Same results; faster for
+                                   such rays, slower for coherent ones (camera grids) */
 };
 /* rays: n records of 8 floats (origin.xyz, unused, direction.xyz, unused) in device memory.
  * hits: n float4 (t, u, v, triangle) with t = FLT_MAX (0x1.fffffep+127) on a miss and the

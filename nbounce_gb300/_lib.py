@@ -29,6 +29,7 @@ NB_ENV_EQUIRECT = 1
 NB_ENV_CUBE = 2
 NB_TRACE_CLOSEST = 0
 NB_TRACE_ANY = 1
+NB_TRACE_INCOHERENT = 2
 NB_SAMPLE_ENV_NEE = 1
 NB_JOB_ENV_NEE = 1
 NB_JOB_CACHE = 2

@@ -905,11 +905,14 @@ int nb_scene_status(const nb_scene* scene, uint32_t* status, void* stream) {
 int nb_trace_rays(const nb_scene* scene, const float* rays, size_t n, uint32_t flags, float* hits,
                   uint32_t* instances, void* stream) {
   if (!scene || (n && (!rays || !hits))) return fail(NB_ERR_INVALID_ARG, "NULL argument");
+  if (flags & ~(uint32_t)(NB_TRACE_ANY | NB_TRACE_INCOHERENT))
+    return fail(NB_ERR_INVALID_ARG, "unknown trace flags 0x%x", flags);
   if (n > 0xFFFFFFE0ull) return fail(NB_ERR_INVALID_ARG, "too many rays in one call");
   if (!scene->uploaded) return fail(NB_ERR_INVALID_ARG, "scene was built with NB_SCENE_HOST_ONLY");
   cudaStream_t st = (cudaStream_t)stream;
   NB_CUDA(cudaMemsetAsync(scene->d_status, 0, sizeof(uint32_t), st), "cudaMemsetAsync");
-  cudaError_t e = launch_trace_rays(scene->dev, rays, (uint32_t)n, (flags & NB_TRACE_ANY) != 0, hits, instances,
+  cudaError_t e = launch_trace_rays(scene->dev, rays, (uint32_t)n, (flags & NB_TRACE_ANY) != 0,
+                                    (flags & NB_TRACE_INCOHERENT) != 0, hits, instances,
                                     scene->d_fetch, scene->d_status, scene->sms, st);
   if (e != cudaSuccess) return cuda_fail(e, "trace launch");
   return NB_OK;

@@ -320,27 +320,93 @@ __device__ __forceinline__ uint32_t trace_ray(const DevScene& s, const V3 wo, co
   return t.status;
 }
 
+// Traces rays 0 .. n-1 of a queue with one warp, refilling lanes: a lane whose ray finished
+// takes a new one once kRefillIdle lanes of the warp are idle (a whole idle warp always takes
+// 32), all of them with one atomic on *fetch.  load(r, o, d, sidx) reads ray r and its scene
+// index; scene(sidx) gives that scene; finish(r, t_hit, uv, tri_inst) consumes ray r's hit
+// record (t = kNoHit on a miss).  Every lane of the warp must call it.  Returns the status
+// bits its rays raised.  Used where the rays of a warp are incoherent (secondary and shadow
+// rays, caller rays): their traversal lengths differ widely, and without refill most lanes
+// would idle while the longest ray of each 32 finishes.  Refill changes only which lane traces
+// a ray, not its result.
+constexpr uint32_t kRefillIdle = 8;
+template <bool kAny, bool kCount, class Load, class SceneOf, class Finish>
+__device__ __forceinline__ uint32_t trace_refill(uint32_t* fetch, uint32_t n, Load load, SceneOf scene, Finish finish,
+                                                 TraceCount* cnt) {
+  const uint32_t lane = threadIdx.x & 31u;
+  TraceState t;
+  uint2 stack[kStackSize + 2];
+  constexpr uint32_t kNone = 0xFFFFFFFFu;
+  uint32_t my = kNone, sidx = 0, st = 0;  // this lane's ray (queue index) and its scene
+  bool exhausted = false;                 // warp-uniform: the queue has no rays left to take
+  uint32_t idle = 0xFFFFFFFFu;            // lanes without a ray
+  while (true) {
+    if (!exhausted && (uint32_t)__popc(idle) >= (idle == 0xFFFFFFFFu ? 1u : kRefillIdle)) {
+      const uint32_t want = (uint32_t)__popc(idle);
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(fetch, want);
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (base + want >= n) exhausted = true;
+      if (my == kNone) {
+        const uint32_t r = base + (uint32_t)__popc(idle & ((1u << lane) - 1u));
+        if (r < n) {
+          my = r;
+          V3 o, d;
+          load(r, o, d, sidx);
+          trace_begin(t, stack, scene(sidx), o, d);
+        }
+      }
+    }
+    if (my != kNone && !trace_step<kAny, kCount>(t, stack, scene(sidx), cnt)) {
+      finish(my, t.t_hit, stack[kHitSlot], stack[kHitSlot + 1]);
+      st |= t.status;
+      my = kNone;
+    }
+    idle = __ballot_sync(0xFFFFFFFFu, my == kNone);
+    if (exhausted && idle == 0xFFFFFFFFu) break;
+  }
+  return st;
+}
+
 // ------------------------------------------------------------------------------------------
 // traversal-only query (nb_trace_rays)
 // ------------------------------------------------------------------------------------------
-template <bool kAny>
+// kRefill: lanes refill as they finish (trace_refill), for rays whose neighbours in the array
+// are unrelated; else each warp traces 32 consecutive rays to the end.
+template <bool kAny, bool kRefill>
 __global__ void __launch_bounds__(128) k_trace_rays(DevScene s, const float4* __restrict__ rays, uint32_t n,
                                                      float4* __restrict__ hits, uint32_t* __restrict__ inst,
                                                      uint32_t* __restrict__ fetch, uint32_t* __restrict__ status) {
   const int lane = threadIdx.x & 31;
   uint32_t st = 0;
-  while (true) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(fetch, 32u);
-    base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    if (base >= n) break;
-    const uint32_t i = base + lane;
-    if (i < n) {
-      const float4 o = __ldg(rays + 2 * (size_t)i), d = __ldg(rays + 2 * (size_t)i + 1);
-      Hit h;
-      st |= trace_ray<kAny>(s, xyz(o), xyz(d), h);
-      hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
-      if (inst) inst[i] = h.inst;
+  if (kRefill) {
+    st = trace_refill<kAny, false>(
+        fetch, n,
+        [&](uint32_t r, V3& o, V3& d, uint32_t& sidx) {
+          o = xyz(__ldg(rays + 2 * (size_t)r));
+          d = xyz(__ldg(rays + 2 * (size_t)r + 1));
+          sidx = 0;
+        },
+        [&](uint32_t) -> const DevScene& { return s; },
+        [&](uint32_t r, float t_hit, uint2 uv, uint2 ti) {
+          hits[r] = make_float4(t_hit, __uint_as_float(uv.x), __uint_as_float(uv.y), __uint_as_float(ti.x));
+          if (inst) inst[r] = ti.y;
+        },
+        nullptr);
+  } else {
+    while (true) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(fetch, 32u);
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (base >= n) break;
+      const uint32_t i = base + lane;
+      if (i < n) {
+        const float4 o = __ldg(rays + 2 * (size_t)i), d = __ldg(rays + 2 * (size_t)i + 1);
+        Hit h;
+        st |= trace_ray<kAny>(s, xyz(o), xyz(d), h);
+        hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
+        if (inst) inst[i] = h.inst;
+      }
     }
   }
   if (st) atomicOr(status, st);
@@ -470,7 +536,16 @@ __global__ void __launch_bounds__(256) k_raygen(PathBatch pb, const WaveTables w
 // unrelated rays, with or without a warp-wide sync per node step, measured 11-30% slower.
 // kCount: the instrumented variant, which also adds the TraceCount totals of the launch to
 // counters[8 * bounce + 0..4] (run only when a caller asks for the counters).
-template <bool kSingle, bool kCount>
+//
+// kRefill (bounces >= 1): a lane whose ray finished does not wait for the rest of its warp's
+// 32 rays; once kRefillIdle lanes of the warp are idle, the warp takes that many new rays with
+// one atomic and those lanes start on them.  Secondary rays of a warp come from different
+// pixels and surfaces and their traversal lengths differ widely, so without refill most lanes
+// idle while the longest ray finishes (11 of 32 lanes active per instruction on bounce 1).
+// Camera rays keep whole-warp chunks: a warp's 32 samples of one pixel finish together, and
+// refilling them measured 9% slower traversal.  Refill changes only which lane traces a ray,
+// not its result.
+template <bool kSingle, bool kCount, bool kRefill>
 __global__ void __launch_bounds__(128, 7) k_trace_wave(PathBatch pb, const WaveTables wt, uint32_t bounce,
                                                        unsigned long long* __restrict__ ray_total,
                                                        unsigned long long* __restrict__ counters) {
@@ -485,20 +560,38 @@ __global__ void __launch_bounds__(128, 7) k_trace_wave(PathBatch pb, const WaveT
   const int lane = threadIdx.x & 31;
   uint32_t st = 0;
   TraceCount cnt;
-  while (true) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(pb.fetch + bounce, 32u);
-    base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    if (base >= n) break;
-    const uint32_t i = base + lane;
-    if (i < n) {
-      const float4 o = qo[i], d = qd[i];
-      Hit h;
-      st |= trace_ray<false, kCount>(kSingle ? wt.scenes[0] : scenes[__float_as_uint(d.w)], xyz(o), xyz(d), h,
-                                     &cnt);
-      pb.hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
-      pb.hit_inst[i] = h.inst;
+  if (!kRefill) {
+    while (true) {
+      uint32_t base = 0;
+      if (lane == 0) base = atomicAdd(pb.fetch + bounce, 32u);
+      base = __shfl_sync(0xFFFFFFFFu, base, 0);
+      if (base >= n) break;
+      const uint32_t i = base + lane;
+      if (i < n) {
+        const float4 o = qo[i], d = qd[i];
+        Hit h;
+        st |= trace_ray<false, kCount>(kSingle ? wt.scenes[0] : scenes[__float_as_uint(d.w)], xyz(o), xyz(d), h,
+                                       &cnt);
+        pb.hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
+        pb.hit_inst[i] = h.inst;
+      }
     }
+  } else {
+    const DevScene* sc = kSingle ? wt.scenes : scenes;
+    st = trace_refill<false, kCount>(
+        pb.fetch + bounce, n,
+        [&](uint32_t r, V3& o, V3& d, uint32_t& sidx) {
+          const float4 o4 = qo[r], d4 = qd[r];
+          o = xyz(o4);
+          d = xyz(d4);
+          sidx = kSingle ? 0u : __float_as_uint(d4.w);
+        },
+        [&](uint32_t sidx) -> const DevScene& { return sc[sidx]; },
+        [&](uint32_t r, float t_hit, uint2 uv, uint2 ti) {
+          pb.hits[r] = make_float4(t_hit, __uint_as_float(uv.x), __uint_as_float(uv.y), __uint_as_float(ti.x));
+          pb.hit_inst[r] = ti.y;
+        },
+        &cnt);
   }
   if (st) atomicOr(pb.status, st);
   if (kCount) {
@@ -1329,8 +1422,8 @@ __global__ void __launch_bounds__(kShadeExtThreads) k_shade_nee(PathBatch pb, co
 }
 
 // Shadow rays of one bounce: an any-hit query each (raytracing_sw.wgsl's triangle test and
-// BIAS, so the ray leaves its own surface like the reference's extension rays); unoccluded
-// rays add their contribution to the path.  A path has at most one shadow ray per bounce, so
+// BIAS, so the ray leaves its own surface like the reference's extension rays), with lane
+// refill (trace_refill); unoccluded rays add their contribution to the path.  A path has at most one shadow ray per bounce, so
 // each radiance entry has one writer per launch.  .w of a shadow ray's direction is the index
 // of its scene in the wave.
 __global__ void __launch_bounds__(128) k_trace_shadow(PathBatch pb, const WaveTables wt, const ShadowQueue sq,
@@ -1339,25 +1432,23 @@ __global__ void __launch_bounds__(128) k_trace_shadow(PathBatch pb, const WaveTa
   for (uint32_t i = threadIdx.x; i < wt.n_scenes; i += blockDim.x) scenes[i] = wt.scenes[i];
   __syncthreads();
   const uint32_t n = sq.counts[bounce];
-  const int lane = threadIdx.x & 31;
-  uint32_t st = 0;
-  while (true) {
-    uint32_t base = 0;
-    if (lane == 0) base = atomicAdd(sq.fetch + bounce, 32u);
-    base = __shfl_sync(0xFFFFFFFFu, base, 0);
-    if (base >= n) break;
-    const uint32_t i = base + lane;
-    if (i < n) {
-      const float4 o = sq.o[i], d = sq.d[i];
-      Hit h;
-      st |= trace_ray<true>(scenes[__float_as_uint(d.w)], xyz(o), xyz(d), h);
-      if (h.t == kNoHit) {
-        const uint32_t id = __float_as_uint(o.w);
-        const float4 c = sq.c[i], r = pb.radiance[id];
-        pb.radiance[id] = make_float4(r.x + c.x, r.y + c.y, r.z + c.z, 0.0f);
-      }
-    }
-  }
+  const uint32_t st = trace_refill<true, false>(
+      sq.fetch + bounce, n,
+      [&](uint32_t r, V3& o, V3& d, uint32_t& sidx) {
+        const float4 d4 = sq.d[r];
+        o = xyz(sq.o[r]);
+        d = xyz(d4);
+        sidx = __float_as_uint(d4.w);
+      },
+      [&](uint32_t sidx) -> const DevScene& { return scenes[sidx]; },
+      [&](uint32_t r, float t_hit, uint2, uint2) {
+        if (t_hit == kNoHit) {
+          const uint32_t id = __float_as_uint(sq.o[r].w);
+          const float4 c = sq.c[r], rr = pb.radiance[id];
+          pb.radiance[id] = make_float4(rr.x + c.x, rr.y + c.y, rr.z + c.z, 0.0f);
+        }
+      },
+      nullptr);
   if (st) atomicOr(pb.status, st);
 }
 
@@ -1403,18 +1494,23 @@ static int blocks_for(const void* kernel, int threads, int sms) {
   return per_sm * sms;
 }
 
-cudaError_t launch_trace_rays(const nbd::DevScene& s, const float* rays, uint32_t n, bool any, float* hits,
-                              uint32_t* inst, uint32_t* fetch, uint32_t* status, int sms, cudaStream_t st) {
+cudaError_t launch_trace_rays(const nbd::DevScene& s, const float* rays, uint32_t n, bool any, bool refill,
+                              float* hits, uint32_t* inst, uint32_t* fetch, uint32_t* status, int sms,
+                              cudaStream_t st) {
   cudaError_t e = cudaMemsetAsync(fetch, 0, sizeof(uint32_t), st);
   if (e != cudaSuccess) return e;
   if (n == 0) return cudaSuccess;
-  if (any) {
-    static const int g = blocks_for((const void*)nbd::k_trace_rays<true>, 128, sms);
-    nbd::k_trace_rays<true><<<g, 128, 0, st>>>(s, (const float4*)rays, n, (float4*)hits, inst, fetch, status);
-  } else {
-    static const int g = blocks_for((const void*)nbd::k_trace_rays<false>, 128, sms);
-    nbd::k_trace_rays<false><<<g, 128, 0, st>>>(s, (const float4*)rays, n, (float4*)hits, inst, fetch, status);
+#define NB_TRACE_RAYS(A, R)                                                                            \
+  {                                                                                                    \
+    static const int g = blocks_for((const void*)nbd::k_trace_rays<A, R>, 128, sms);                  \
+    nbd::k_trace_rays<A, R><<<g, 128, 0, st>>>(s, (const float4*)rays, n, (float4*)hits, inst, fetch, status); \
   }
+  if (any) {
+    if (refill) NB_TRACE_RAYS(true, true) else NB_TRACE_RAYS(true, false)
+  } else {
+    if (refill) NB_TRACE_RAYS(false, true) else NB_TRACE_RAYS(false, false)
+  }
+#undef NB_TRACE_RAYS
   return cudaGetLastError();
 }
 
@@ -1427,21 +1523,24 @@ cudaError_t launch_raygen(const PathBatch& pb, const WaveTables& wt, int sms, cu
 cudaError_t launch_trace_wave(const PathBatch& pb, const WaveTables& wt, bool single_scene, uint32_t bounce,
                               unsigned long long* ray_total, int sms, cudaStream_t st,
                               unsigned long long* counters) {
+  const bool refill = bounce >= 1;
+#define NB_TRACE_WAVE(S, C, R)                                                                \
+  {                                                                                           \
+    static const int g = blocks_for((const void*)nbd::k_trace_wave<S, C, R>, 128, sms);       \
+    nbd::k_trace_wave<S, C, R><<<g, 128, 0, st>>>(pb, wt, bounce, ray_total, counters);      \
+  }
   if (counters) {
     if (single_scene) {
-      static const int g = blocks_for((const void*)nbd::k_trace_wave<true, true>, 128, sms);
-      nbd::k_trace_wave<true, true><<<g, 128, 0, st>>>(pb, wt, bounce, ray_total, counters);
+      if (refill) NB_TRACE_WAVE(true, true, true) else NB_TRACE_WAVE(true, true, false)
     } else {
-      static const int g = blocks_for((const void*)nbd::k_trace_wave<false, true>, 128, sms);
-      nbd::k_trace_wave<false, true><<<g, 128, 0, st>>>(pb, wt, bounce, ray_total, counters);
+      if (refill) NB_TRACE_WAVE(false, true, true) else NB_TRACE_WAVE(false, true, false)
     }
   } else if (single_scene) {
-    static const int g = blocks_for((const void*)nbd::k_trace_wave<true, false>, 128, sms);
-    nbd::k_trace_wave<true, false><<<g, 128, 0, st>>>(pb, wt, bounce, ray_total, nullptr);
+    if (refill) NB_TRACE_WAVE(true, false, true) else NB_TRACE_WAVE(true, false, false)
   } else {
-    static const int g = blocks_for((const void*)nbd::k_trace_wave<false, false>, 128, sms);
-    nbd::k_trace_wave<false, false><<<g, 128, 0, st>>>(pb, wt, bounce, ray_total, nullptr);
+    if (refill) NB_TRACE_WAVE(false, false, true) else NB_TRACE_WAVE(false, false, false)
   }
+#undef NB_TRACE_WAVE
   return cudaGetLastError();
 }
 

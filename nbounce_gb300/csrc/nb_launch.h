@@ -63,8 +63,10 @@ struct PathBatch {
   uint32_t sobol_entries;
 };
 
-cudaError_t launch_trace_rays(const nbd::DevScene& s, const float* rays, uint32_t n, bool any, float* hits,
-                              uint32_t* inst, uint32_t* fetch, uint32_t* status, int sms, cudaStream_t st);
+// refill: lanes take new rays as theirs finish (for arrays whose neighbouring rays are unrelated)
+cudaError_t launch_trace_rays(const nbd::DevScene& s, const float* rays, uint32_t n, bool any, bool refill,
+                              float* hits, uint32_t* inst, uint32_t* fetch, uint32_t* status, int sms,
+                              cudaStream_t st);
 
 cudaError_t launch_raygen(const PathBatch& pb, const WaveTables& wt, int sms, cudaStream_t st);
 // single_scene: all paths use wt.scenes[0] (passed by value); otherwise each ray's scene index.

@@ -113,19 +113,24 @@ class SceneBuffers:
         check(lib().nb_scene_export(self._h, ptr(blas), ptr(tlas), ptr(inst), ptr(idx)))
         return dict(blas=blas, tlas=tlas, instances=inst, indices=idx)
 
-    def trace_host(self, rays, any_hit=False, with_instances=True, stream=None):
-        """rays (n, 8) float32 on the host -> (hits (n, 4) float32, instances (n,) u32 or None)."""
+    @staticmethod
+    def _trace_flags(any_hit, incoherent):
+        return (L.NB_TRACE_ANY if any_hit else 0) | (L.NB_TRACE_INCOHERENT if incoherent else 0)
+
+    def trace_host(self, rays, any_hit=False, with_instances=True, stream=None, incoherent=False):
+        """rays (n, 8) float32 on the host -> (hits (n, 4) float32, instances (n,) u32 or None).
+        incoherent: the rays' neighbours are unrelated (lanes refill; same results)."""
         r = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
         n = r.shape[0]
         hits = np.zeros((n, 4), np.float32)
         inst = np.zeros(n, np.uint32) if with_instances else None
-        check(lib().nb_trace_rays_host(self._h, ptr(r), n, L.NB_TRACE_ANY if any_hit else 0, ptr(hits), ptr(inst),
-                                       _stream(stream)))
+        check(lib().nb_trace_rays_host(self._h, ptr(r), n, self._trace_flags(any_hit, incoherent), ptr(hits),
+                                       ptr(inst), _stream(stream)))
         return hits, inst
 
-    def trace_device(self, rays_ptr, n, hits_ptr, inst_ptr=None, any_hit=False, stream=None):
+    def trace_device(self, rays_ptr, n, hits_ptr, inst_ptr=None, any_hit=False, stream=None, incoherent=False):
         """Asynchronous query on device buffers given as integer addresses."""
-        check(lib().nb_trace_rays(self._h, C.c_void_p(rays_ptr), n, L.NB_TRACE_ANY if any_hit else 0,
+        check(lib().nb_trace_rays(self._h, C.c_void_p(rays_ptr), n, self._trace_flags(any_hit, incoherent),
                                   C.c_void_p(hits_ptr), None if inst_ptr is None else C.c_void_p(inst_ptr),
                                   _stream(stream)))
 
