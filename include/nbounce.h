@@ -477,7 +477,7 @@ typedef struct nb_cache_config {
                                    with this decay per step (0.99); 0: the weights themselves */
   float grad_clip;              /* bound on |dloss/doutput| per record and channel (0: none);
                                    limits the pull of rare very bright targets (sun hits) */
-  uint32_t tensor_path;         /* cache lookups on NB_CACHE_TCGEN05 (default) or NB_CACHE_MMA_SYNC */
+  uint32_t tensor_path;         /* lookups and training on NB_CACHE_TCGEN05 (default) or NB_CACHE_MMA_SYNC */
 } nb_cache_config;
 
 enum { NB_CACHE_TCGEN05 = 0, NB_CACHE_MMA_SYNC = 1 };

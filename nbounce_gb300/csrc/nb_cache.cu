@@ -15,7 +15,9 @@
 //   k_cache_infer_*  mma.sync: one warp evaluates 32 rows, the activations never leave
 //                    registers (the C fragment of layer l, ReLU'd and packed to BF16, is the A
 //                    fragment of layer l + 1)
-//   k_cache_grad     one CTA of 8 warps takes 128 rows: forward with the activations kept in
+//   k_cache_grad_tc  tcgen05.mma training (the default path): one warpgroup per 128 rows,
+//                    forward, backward and weight-gradient GEMMs with TMEM accumulators
+//   k_cache_grad     mma.sync training: one CTA of 8 warps takes 128 rows: forward with the activations kept in
 //                    shared memory, relative L2 loss (p - y)^2 / (p^2 + 0.01) with the
 //                    denominator held constant, backward through the 6 layers; each layer's
 //                    weight gradient dZ^T H is a 128-deep GEMM across the CTA's rows written
@@ -317,7 +319,7 @@ constexpr uint32_t kTcWaitLimit = 1u << 22;                    // mbarrier polls
 constexpr uint32_t kStatusCacheTimeout = 1u << 8;
 
 // byte offset of element (row, k) of a canonical K-major operand (rows x 64)
-__device__ __forceinline__ uint32_t canon_off(uint32_t row, uint32_t k) {
+__host__ __device__ __forceinline__ uint32_t canon_off(uint32_t row, uint32_t k) {
   return (row >> 3) * 1024u + (k >> 3) * 128u + (row & 7u) * 16u + (k & 7u) * 2u;
 }
 
@@ -770,6 +772,285 @@ __global__ void __launch_bounds__(256, 1) k_cache_grad(const bf16* __restrict__ 
   }
 }
 
+// ---- training on the 5th-generation tensor cores (tcgen05) -------------------------------
+//
+// One warpgroup per 128-row group (thread = row = tensor-memory lane), every GEMM a
+// tcgen05.mma with M = 128 and FP32 accumulators in tensor memory, issued by one thread and
+// committed to one mbarrier:
+//   forward    Z_{l+1} = H_l W_l^T          A = H_l (rows x in, K-major), B = W_l (out x in)
+//   backward   dH_l = dZ_{l+1} W_l           A = dZ_{l+1} (rows x out), B = W_l^T (in x out)
+//   weights    dW_l = dZ_{l+1}^T H_l         A = dZ_{l+1}, B = H_l, both read through MN-major
+//                                            descriptors (M = out, N = in, K = the 128 rows)
+// so the activations H_0..H_5 and the output gradient are stored once, row-major in the
+// canonical layout, and serve both as K-major operands (rows x features) and as MN-major ones
+// (features x rows).  M is 128 for the weight GEMMs too: rows out >= 64 (>= 16 for the output
+// layer) read whatever follows in shared memory and land in accumulator lanes nobody reads.
+// The backward GEMM of a layer and its weight GEMM read the same dZ and are issued together.
+// Rounding points are those of k_cache_grad (BF16 activations and output gradients, FP32
+// accumulation), and the partials have its layout, so k_cache_adam serves both.
+constexpr uint32_t kTrRows = 128;
+constexpr size_t kTrWf = 5 * 8192 + 2048;              // W_0..W_4 (64 x 64), W_5 (16 x 64)
+constexpr size_t kTrWb = 4 * 8192 + 2048;              // W_1^T..W_4^T (64 x 64), W_5^T (64 x 16)
+constexpr size_t kTrAct = (size_t)kTrRows * 64 * 2;    // one 128 x 64 BF16 tile
+// 128 x 16 output gradient (4 KB) + slack: the padded weight GEMMs read up to ~29 KB past the
+// start of dZ and ~7.5 KB past dZ6, all inside this allocation
+constexpr size_t kTrDz6 = 14336;
+constexpr size_t kTrSmem = kTrWf + kTrWb + 7 * kTrAct + kTrDz6;  // H_0..H_5, dZ: 206,848 B
+constexpr uint32_t kTrCols = 256;                      // TMEM: [0, 64) layer GEMMs, [64, 192) two weight-GEMM buffers
+constexpr size_t kTrStage = kTrWf + kTrWb;             // the weight image the training kernel copies in
+
+// Where parameter p (rows [out][in] per layer) sits in the training kernel's weight image:
+// *f in the forward operands W_l (out x in), *b in the backward ones W_l^T (in x out), or
+// 0xFFFFFFFF for the first layer, whose transpose no GEMM needs.  Adam keeps the image current.
+__host__ __device__ __forceinline__ void stage_offsets(uint32_t p, uint32_t* f, uint32_t* b) {
+  const uint32_t l = p >> 12, r = p & 4095u, out = r >> 6, in = r & 63u;
+  *f = l * 8192u + canon_off(out, in);
+  if (l == 0) *b = 0xFFFFFFFFu;
+  else if (l < 5) *b = (uint32_t)kTrWf + (l - 1u) * 8192u + canon_off(in, out);
+  else *b = (uint32_t)kTrWf + 4u * 8192u + (in >> 3) * 256u + (out >> 3) * 128u + (in & 7u) * 16u + (out & 7u) * 2u;
+}
+
+// shared-memory matrix descriptor with explicit leading / stride byte offsets, no swizzle
+__device__ __forceinline__ uint64_t tc_desc2(uint32_t addr, uint32_t lbo, uint32_t sbo) {
+  return (uint64_t)((addr >> 4) & 0x3FFFu) | ((uint64_t)((lbo >> 4) & 0x3FFFu) << 16) |
+         ((uint64_t)((sbo >> 4) & 0x3FFFu) << 32) | (1ull << 46);
+}
+// kind::f16 instruction descriptor with the operands' major-ness (bit 15: A MN-major, 16: B)
+__host__ __device__ constexpr uint32_t tc_idesc2(uint32_t M, uint32_t N, bool a_mn, bool b_mn) {
+  return tc_idesc(M, N) | (a_mn ? (1u << 15) : 0u) | (b_mn ? (1u << 16) : 0u);
+}
+// A row-major canonical tile (8-feature chunks of 16 B, 8-row groups G bytes apart) read as an
+// MN-major operand (features x rows): leading byte offset G (between 8-row groups, along K),
+// stride byte offset 128 B (between 8-feature chunks, along M or N).
+
+__global__ void __launch_bounds__(128, 1) k_cache_grad_tc(const unsigned char* __restrict__ stage,
+                                                          const bf16* __restrict__ X,
+                                                          const float4* __restrict__ Y,
+                                                          const uint32_t* __restrict__ n_dev, uint32_t n_host,
+                                                          uint32_t row0, uint32_t rows_per_step, float clip,
+                                                          float* __restrict__ part_dw, float* __restrict__ part_loss,
+                                                          uint32_t* __restrict__ status) {
+  extern __shared__ __align__(128) unsigned char smem_tr[];
+  __shared__ __align__(8) uint64_t mbar_slot, copy_slot;
+  __shared__ uint32_t tmem_slot;
+  __shared__ float warp_loss[4];
+  unsigned char* Wf = smem_tr;
+  unsigned char* Wb = Wf + kTrWf;
+  unsigned char* H = Wb + kTrWb;          // H_l at H + l * kTrAct
+  unsigned char* dZ = H + 6 * kTrAct;     // 128 x 64 output gradient of the layer being done
+  unsigned char* dZ6 = dZ + kTrAct;       // 128 x 16 gradient of the output layer
+  const uint32_t tid = threadIdx.x, warp = tid >> 5;
+  const uint32_t mbar = saddr(&mbar_slot);
+  const uint32_t n_total = n_dev ? *n_dev : n_host;
+  const uint32_t end = n_total > row0 ? row0 + min(n_total - row0, rows_per_step) : row0;
+  const uint32_t row = row0 + blockIdx.x * kTrRows + tid;
+  float* dw = part_dw + (size_t)blockIdx.x * kMlpParams;
+
+  // the weight image (W_l and W_l^T already in the canonical layout): bulk asynchronous
+  // copies of 16 KB or less, completing on copy_slot
+  const uint32_t copy_bar = saddr(&copy_slot);
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(copy_bar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;\n" ::"r"(copy_bar), "r"((uint32_t)kTrStage)
+                 : "memory");
+    for (uint32_t off = 0; off < (uint32_t)kTrStage; off += 16384u) {
+      const uint32_t bytes = min(16384u, (uint32_t)kTrStage - off);
+      asm volatile("cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];\n" ::"r"(
+                       saddr(Wf + off)),
+                   "l"(stage + off), "r"(bytes), "r"(copy_bar)
+                   : "memory");
+    }
+  }
+  // this thread's input row
+  {
+    const bool live = row < end;
+#pragma unroll
+    for (uint32_t c = 0; c < 8; ++c) {
+      const uint4 v = live ? __ldg(reinterpret_cast<const uint4*>(X + (size_t)row * 64) + c) : make_uint4(0u, 0u, 0u, 0u);
+      *reinterpret_cast<uint4*>(H + canon_off(tid, 8u * c)) = v;
+    }
+  }
+  if (tid == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;\n" ::"r"(mbar) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;\n" ::: "memory");
+  }
+  if (warp == 0) {
+    __syncwarp();
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;\n" ::"r"(saddr(&tmem_slot)),
+                 "r"(kTrCols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;\n" ::: "memory");
+  }
+  fence_async_smem();
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const bool staged = mbar_wait(copy_bar, 0u);  // the weight image has landed
+  const uint32_t tmem = tmem_slot, lane_base = (32u * warp) << 16;
+  const uint32_t d_layer = tmem;  // weight GEMMs alternate between tmem + 64 and tmem + 128
+  uint32_t phase = 0;
+  bool failed = false;
+  uint32_t fail_round = 0, round = 0;
+
+  // waits for the committed MMAs; every thread learns whether any wait gave up
+  auto wait_all = [&]() {
+    const bool ok = mbar_wait(mbar, phase);
+    phase ^= 1u;
+    ++round;
+    tc_fence_after();
+    return ok;
+  };
+  // ends a round of shared-memory writes that the next MMAs read
+  auto publish = [&](bool bad) {
+    fence_async_smem();
+    tc_fence_before();
+    const bool any_bad = __syncthreads_or(bad ? 1 : 0) != 0;
+    tc_fence_after();
+    if (any_bad && !failed) {
+      failed = true;
+      fail_round = round;
+    }
+  };
+  publish(!staged);
+
+  // ---- forward: H_1..H_5, then the output layer
+  for (int l = 0; l < 6 && !failed; ++l) {
+    if (tid == 0) {
+      const uint32_t a = saddr(H + l * kTrAct), b = saddr(Wf + l * 8192u);
+      const uint32_t idesc = tc_idesc(kTrRows, l < 5 ? 64u : 16u);
+#pragma unroll
+      for (uint32_t k = 0; k < 4; ++k)
+        tc_mma(d_layer, tc_desc2(a + 256u * k, 128u, 1024u), tc_desc2(b + 256u * k, 128u, 1024u), idesc, k);
+      tc_commit(mbar);
+    }
+    const bool ok = wait_all();
+    if (l < 5) {
+      unsigned char* h = H + (l + 1) * kTrAct;
+#pragma unroll
+      for (uint32_t c4 = 0; c4 < 4; ++c4) {
+        float v[16];
+        tc_ld16(d_layer + lane_base + 16u * c4, v);
+        *reinterpret_cast<uint4*>(h + canon_off(tid, 16u * c4)) =
+            make_uint4(pack2(relu(v[0]), relu(v[1])), pack2(relu(v[2]), relu(v[3])), pack2(relu(v[4]), relu(v[5])),
+                       pack2(relu(v[6]), relu(v[7])));
+        *reinterpret_cast<uint4*>(h + canon_off(tid, 16u * c4 + 8u)) =
+            make_uint4(pack2(relu(v[8]), relu(v[9])), pack2(relu(v[10]), relu(v[11])),
+                       pack2(relu(v[12]), relu(v[13])), pack2(relu(v[14]), relu(v[15])));
+      }
+    } else {
+      // output layer: dL/dp = 2 (p - y) / (p^2 + 0.01) with the denominator held constant
+      float v[16];
+      tc_ld16(d_layer + lane_base, v);
+      float gz[3] = {0.0f, 0.0f, 0.0f}, lsum = 0.0f;
+      if (row < end) {
+        const float4 y4 = __ldg(Y + row);
+        if (y4.w != 0.0f) {
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            const float y = c == 0 ? y4.x : (c == 1 ? y4.y : y4.z);
+            const float d = v[c] - y;
+            const float den = v[c] * v[c] + 0.01f;
+            lsum += d * d / den;
+            gz[c] = 2.0f * d / den;
+            if (clip > 0.0f) gz[c] = fminf(fmaxf(gz[c], -clip), clip);
+          }
+        }
+      }
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) lsum += __shfl_xor_sync(0xFFFFFFFFu, lsum, o);
+      if ((tid & 31u) == 0) warp_loss[warp] = lsum;
+      // dZ6: 128 x 16 (outputs 3..15 zero), 8-row groups 256 B apart
+      unsigned char* d6 = dZ6 + (tid >> 3) * 256u + (tid & 7u) * 16u;
+      *reinterpret_cast<uint4*>(d6) = make_uint4(pack2(gz[0], gz[1]), pack2(gz[2], 0.0f), 0u, 0u);
+      *reinterpret_cast<uint4*>(d6 + 128u) = make_uint4(0u, 0u, 0u, 0u);
+    }
+    publish(!ok);
+  }
+
+  // ---- backward: layer 5 (16 x 64), then 4 .. 0 (64 x 64).  The MMAs of layer l - 1 are
+  // issued as soon as dZ_l is in shared memory; meanwhile the warps read layer l's weight
+  // gradient out of the other tensor-memory buffer and store it.
+  // issues dH_l = dZ_{l+1} W_l (l >= 1) and dW_l = dZ_{l+1}^T H_l, then commits
+  auto issue_backward = [&](int l) {
+    if (tid != 0) return;
+    const bool out_layer = l == 5;
+    const uint32_t dz_group = out_layer ? 256u : 1024u;  // bytes between 8-row groups of dZ
+    const uint32_t a = saddr(out_layer ? dZ6 : dZ), h = saddr(H + l * kTrAct);
+    if (l >= 1) {  // K = 16 (output layer) or 64
+      const uint32_t b = out_layer ? saddr(Wb + 4u * 8192u) : saddr(Wb + (l - 1) * 8192u);
+      const uint32_t idesc = tc_idesc(kTrRows, 64u);
+      const uint32_t kk = out_layer ? 1u : 4u;
+      for (uint32_t k = 0; k < kk; ++k)
+        tc_mma(d_layer, tc_desc2(a + 256u * k, 128u, dz_group), tc_desc2(b + 256u * k, 128u, out_layer ? 256u : 1024u),
+               idesc, k);
+    }
+    // M = out (padded to 128), N = in, K = 128 rows in 8 steps of 16
+    const uint32_t d_w = tmem + 64u + 64u * (uint32_t)(l & 1);
+    const uint32_t idesc = tc_idesc2(kTrRows, 64u, true, true);
+#pragma unroll
+    for (uint32_t k = 0; k < 8; ++k)
+      tc_mma(d_w, tc_desc2(a + 2u * k * dz_group, dz_group, 128u), tc_desc2(h + 2u * k * 1024u, 1024u, 128u), idesc, k);
+    tc_commit(mbar);
+  };
+  if (!failed) issue_backward(5);
+  for (int l = 5; l >= 0 && !failed; --l) {
+    const bool ok = wait_all();
+    if (l >= 1) {
+      // dZ_l = dH_l where H_l > 0 (BF16 activation), written over dZ (its MMAs are complete)
+      const unsigned char* hl = H + l * kTrAct;
+#pragma unroll
+      for (uint32_t c4 = 0; c4 < 4; ++c4) {
+        float v[16];
+        tc_ld16(d_layer + lane_base + 16u * c4, v);
+        const uint4 m0 = *reinterpret_cast<const uint4*>(hl + canon_off(tid, 16u * c4));
+        const uint4 m1 = *reinterpret_cast<const uint4*>(hl + canon_off(tid, 16u * c4 + 8u));
+        *reinterpret_cast<uint4*>(dZ + canon_off(tid, 16u * c4)) =
+            make_uint4(pack2(gate_lo(v[0], m0.x), gate_hi(v[1], m0.x)), pack2(gate_lo(v[2], m0.y), gate_hi(v[3], m0.y)),
+                       pack2(gate_lo(v[4], m0.z), gate_hi(v[5], m0.z)), pack2(gate_lo(v[6], m0.w), gate_hi(v[7], m0.w)));
+        *reinterpret_cast<uint4*>(dZ + canon_off(tid, 16u * c4 + 8u)) =
+            make_uint4(pack2(gate_lo(v[8], m1.x), gate_hi(v[9], m1.x)), pack2(gate_lo(v[10], m1.y), gate_hi(v[11], m1.y)),
+                       pack2(gate_lo(v[12], m1.z), gate_hi(v[13], m1.z)),
+                       pack2(gate_lo(v[14], m1.w), gate_hi(v[15], m1.w)));
+      }
+    }
+    publish(!ok);
+    if (l >= 1 && !failed) issue_backward(l - 1);
+    // weight gradient of layer l: accumulator lane = output unit (< 16 or < 64 live), columns =
+    // inputs; warps without live units skip the (warp-collective) loads
+    if (!failed && 32u * warp < (l == 5 ? 16u : 64u)) {
+      const uint32_t outs = l == 5 ? 16u : 64u;
+      const uint32_t d_w = tmem + 64u + 64u * (uint32_t)(l & 1);
+      float* d = dw + (size_t)l * 4096u + (size_t)tid * 64u;
+#pragma unroll
+      for (uint32_t c4 = 0; c4 < 4; ++c4) {
+        float v[16];
+        tc_ld16(d_w + lane_base + 16u * c4, v);
+        if (tid < outs) {
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+            *reinterpret_cast<float4*>(d + 16u * c4 + 4u * q) = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
+        }
+      }
+    }
+    // the next round's epilogue overwrites dZ only after its wait, i.e. after these loads
+  }
+  if (tid == 0) {
+    part_loss[blockIdx.x] = warp_loss[0] + warp_loss[1] + warp_loss[2] + warp_loss[3];
+    if (failed) {
+      atomicOr(status, kStatusCacheTimeout | ((100u + fail_round) << 16));
+      mbar_wait(mbar, phase ^ 1u);  // give MMAs still in flight a bounded chance to finish
+    }
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    __syncwarp();
+    tc_fence_after();
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;\n" ::"r"(tmem_slot), "r"(kTrCols) : "memory");
+  }
+}
+
 struct AdamArgs {
   float lr, beta1, beta2, eps;
   float bc1, bc2;  // 1 - beta^t
@@ -778,10 +1059,14 @@ struct AdamArgs {
   int update;
 };
 
-// Sums the per-CTA partials in CTA order and applies one Adam step (update != 0), or only
-// writes the mean gradient to grad_out.  With ema > 0 it also advances the weight average
-// that renders query (Mueller et al. 2021 average the weights the same way).
+// Sums the per-CTA partials and applies one Adam step (update != 0), or only writes the mean
+// gradient to grad_out.  A block takes 32 parameters: its 8 warps each sum every 8th partial
+// (partials k, k + 8, ... for warp k, two running sums), and the 8 sums are combined in a fixed
+// order, so the result does not depend on scheduling.  With ema > 0 it also advances the
+// weight average that renders query (Mueller et al. 2021 average the weights the same way).
+constexpr uint32_t kAdamParams = 32;  // parameters per block (one per lane)
 __global__ void __launch_bounds__(256) k_cache_adam(float* __restrict__ w, bf16* __restrict__ wb,
+                                                    unsigned char* __restrict__ stage,
                                                     float* __restrict__ we, bf16* __restrict__ web,
                                                     float* __restrict__ m, float* __restrict__ v,
                                                     const float* __restrict__ part_dw,
@@ -789,25 +1074,32 @@ __global__ void __launch_bounds__(256) k_cache_adam(float* __restrict__ w, bf16*
                                                     const uint32_t* __restrict__ n_dev, uint32_t n_host,
                                                     uint32_t row0, uint32_t rows_per_step, AdamArgs args,
                                                     float* __restrict__ grad_out, float* __restrict__ loss_out) {
+  __shared__ float red[8][kAdamParams];
   const uint32_t n_total = n_dev ? *n_dev : n_host;
   const uint32_t rows = n_total > row0 ? min(n_total - row0, rows_per_step) : 0u;
-  const uint32_t p = blockIdx.x * blockDim.x + threadIdx.x;
+  const uint32_t lane = threadIdx.x & 31u, grp = threadIdx.x >> 5;
+  const uint32_t p = blockIdx.x * kAdamParams + lane;
   const uint32_t parts = (rows + kGradRows - 1) / kGradRows;
   const float scale = rows ? 1.0f / (3.0f * (float)rows) : 0.0f;
-  if (p == 0 && loss_out) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && loss_out) {
     float s = 0.0f;
     for (uint32_t c = 0; c < parts; ++c) s += part_loss[c];
     *loss_out = s * scale;
   }
-  if (p >= (uint32_t)kMlpParams) return;
-  // eight independent partial sums keep eight loads in flight; combined in a fixed order
-  float acc[8] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
-  uint32_t c = 0;
-  for (; c + 8 <= parts; c += 8)
-#pragma unroll
-    for (int k = 0; k < 8; ++k) acc[k] += part_dw[(size_t)(c + k) * kMlpParams + p];
-  for (; c < parts; ++c) acc[c & 7u] += part_dw[(size_t)c * kMlpParams + p];
-  const float gsum = ((acc[0] + acc[1]) + (acc[2] + acc[3])) + ((acc[4] + acc[5]) + (acc[6] + acc[7]));
+  float a0 = 0.0f, a1 = 0.0f;
+  if (p < (uint32_t)kMlpParams) {
+    uint32_t c = grp;
+    for (; c + 8 < parts; c += 16) {
+      a0 += part_dw[(size_t)c * kMlpParams + p];
+      a1 += part_dw[(size_t)(c + 8) * kMlpParams + p];
+    }
+    if (c < parts) a0 += part_dw[(size_t)c * kMlpParams + p];
+  }
+  red[grp][lane] = a0 + a1;
+  __syncthreads();
+  if (grp != 0 || p >= (uint32_t)kMlpParams) return;
+  const float gsum = ((red[0][lane] + red[1][lane]) + (red[2][lane] + red[3][lane])) +
+                     ((red[4][lane] + red[5][lane]) + (red[6][lane] + red[7][lane]));
   const bool live = p < kLiveEnd;
   const float gr = live ? gsum * scale : 0.0f;
   if (grad_out) grad_out[p] = gr;
@@ -818,7 +1110,12 @@ __global__ void __launch_bounds__(256) k_cache_adam(float* __restrict__ w, bf16*
   v[p] = vv;
   const float wn = w[p] - args.lr * (mm / args.bc1) / (sqrtf(vv / args.bc2) + args.eps);
   w[p] = wn;
-  wb[p] = __float2bfloat16_rn(wn);
+  const bf16 b16 = __float2bfloat16_rn(wn);
+  wb[p] = b16;
+  uint32_t of, ob;
+  stage_offsets(p, &of, &ob);
+  *reinterpret_cast<bf16*>(stage + of) = b16;
+  if (ob != 0xFFFFFFFFu) *reinterpret_cast<bf16*>(stage + ob) = b16;
   if (args.ema > 0.0f) {
     const float e = args.ema * we[p] + (1.0f - args.ema) * wn;
     we[p] = e;
@@ -1006,7 +1303,8 @@ struct nb_cache {
   nbd::bf16* web = nullptr;
   float* m = nullptr;
   float* v = nullptr;
-  uint32_t* status = nullptr;  // tensor-core wait timeouts of nb_cache_infer
+  uint32_t* status = nullptr;  // tensor-core wait timeouts of nb_cache_infer / training
+  unsigned char* wstage = nullptr;  // training weight image (k_cache_grad_tc), kept by k_cache_adam
   float* part_dw = nullptr;
   float* part_loss = nullptr;
   uint32_t part_cap = 0;  // CTAs the partial buffers hold
@@ -1068,6 +1366,9 @@ int set_smem_limits() {
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(nbd::k_cache_infer_tc<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)nbd::kTcSmem);
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(nbd::k_cache_grad_tc, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)nbd::kTrSmem);
     rc = e == cudaSuccess ? NB_OK : cuda_fail(e, "cudaFuncSetAttribute(cache kernels)");
   });
   return rc;
@@ -1082,6 +1383,14 @@ int upload_weights(nb_cache* c, const float* w_host) {
   NB_CUDA(cudaMemcpy(c->web, b.data(), kMlpParams * sizeof(nbd::bf16), cudaMemcpyHostToDevice), "cudaMemcpy(weights)");
   NB_CUDA(cudaMemset(c->m, 0, kMlpParams * sizeof(float)), "cudaMemset");
   NB_CUDA(cudaMemset(c->v, 0, kMlpParams * sizeof(float)), "cudaMemset");
+  std::vector<unsigned char> img(nbd::kTrStage, 0);
+  for (uint32_t p = 0; p < (uint32_t)kMlpParams; ++p) {
+    uint32_t of, ob;
+    nbd::stage_offsets(p, &of, &ob);
+    std::memcpy(img.data() + of, &b[p], sizeof(nbd::bf16));
+    if (ob != 0xFFFFFFFFu) std::memcpy(img.data() + ob, &b[p], sizeof(nbd::bf16));
+  }
+  NB_CUDA(cudaMemcpy(c->wstage, img.data(), img.size(), cudaMemcpyHostToDevice), "cudaMemcpy(weight image)");
   c->adam_steps = 0;
   return NB_OK;
 }
@@ -1136,8 +1445,12 @@ cudaError_t train_launch(nb_cache* c, const nbd::bf16* X, const float4* Y, const
                          uint32_t row0, uint32_t rows_per_step, bool update, float* grad_out, float* loss_out,
                          cudaStream_t st) {
   const uint32_t ctas = (rows_per_step + nbd::kGradRows - 1) / nbd::kGradRows;
-  nbd::k_cache_grad<<<ctas, 256, nbd::kGradSmem, st>>>(c->wb, X, Y, n_dev, n_host, row0, rows_per_step,
-                                                       c->cfg.grad_clip, c->part_dw, c->part_loss);
+  if (c->cfg.tensor_path == NB_CACHE_TCGEN05)
+    nbd::k_cache_grad_tc<<<ctas, 128, nbd::kTrSmem, st>>>(c->wstage, X, Y, n_dev, n_host, row0, rows_per_step,
+                                                          c->cfg.grad_clip, c->part_dw, c->part_loss, c->status);
+  else
+    nbd::k_cache_grad<<<ctas, 256, nbd::kGradSmem, st>>>(c->wb, X, Y, n_dev, n_host, row0, rows_per_step,
+                                                         c->cfg.grad_clip, c->part_dw, c->part_loss);
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return e;
   nbd::AdamArgs a{};
@@ -1158,7 +1471,9 @@ cudaError_t train_launch(nb_cache* c, const nbd::bf16* X, const float4* Y, const
   } else {
     a.bc1 = a.bc2 = a.ec = 1.0f;
   }
-  nbd::k_cache_adam<<<(kMlpParams + 255) / 256, 256, 0, st>>>(c->w, c->wb, c->we, c->web, c->m, c->v, c->part_dw,
+  nbd::k_cache_adam<<<(kMlpParams + nbd::kAdamParams - 1) / nbd::kAdamParams, 256, 0, st>>>(
+      c->w, c->wb, c->wstage, c->we, c->web, c->m, c->v,
+                                                              c->part_dw,
                                                               c->part_loss,
                                                               n_dev, n_host, row0, rows_per_step, a, grad_out,
                                                               loss_out);
@@ -1352,6 +1667,9 @@ int nb_cache_create(const nb_cache_config* cfg, nb_cache** out) {
   h->v = (float*)p[5];
   if (!rc) rc = h->arena.alloc(sizeof(uint32_t), &p[6]);
   h->status = (uint32_t*)p[6];
+  void* stage = nullptr;
+  if (!rc) rc = h->arena.alloc(nbd::kTrStage, &stage);
+  h->wstage = (unsigned char*)stage;
   if (!rc) {
     // He-uniform initialisation: U(-sqrt(6 / 64), sqrt(6 / 64)); padding rows of W_5 zero
     std::vector<float> w(kMlpParams, 0.0f);
@@ -1468,14 +1786,21 @@ static int rows_op(nb_cache* c, const float* enc, const float* target, size_t n,
   if ((rc = ensure_parts(c, ctas)) || (rc = ensure_losses(c, 1))) return rc;
   cudaStream_t st = (cudaStream_t)stream;
   const int sms = sm_count();
-  nbd::k_to_bf16<<<grid_for(n * 64, 256, sms), 256, 0, st>>>(enc, c->sx, n * 64);
-  nbd::k_targets<<<grid_for(n, 256, sms), 256, 0, st>>>(target, c->sy, n);
-  cudaError_t e = cudaGetLastError();
+  const bool tc = c->cfg.tensor_path == NB_CACHE_TCGEN05;
+  cudaError_t e = tc ? cudaMemsetAsync(c->status, 0, sizeof(uint32_t), st) : cudaSuccess;
+  if (e == cudaSuccess) {
+    nbd::k_to_bf16<<<grid_for(n * 64, 256, sms), 256, 0, st>>>(enc, c->sx, n * 64);
+    nbd::k_targets<<<grid_for(n, 256, sms), 256, 0, st>>>(target, c->sy, n);
+    e = cudaGetLastError();
+  }
   if (e == cudaSuccess)
     e = train_launch(c, c->sx, c->sy, nullptr, (uint32_t)n, 0, (uint32_t)n, update, grad, c->losses, st);
   if (e == cudaSuccess && loss) e = cudaMemcpyAsync(loss, c->losses, sizeof(float), cudaMemcpyDeviceToHost, st);
+  uint32_t status = 0;
+  if (e == cudaSuccess && tc) e = cudaMemcpyAsync(&status, c->status, sizeof(status), cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_fail(e, "cache training launch");
+  if (status & nbd::kStatusCacheTimeout) return fail(NB_ERR_TIMEOUT, "tensor-core wait timed out in training");
   return NB_OK;
 }
 

@@ -65,9 +65,12 @@ def test_infer_matches_reference(path):
     assert rel(out.cpu().numpy(), ref32.numpy()) < FP32_REL
 
 
+@pytest.mark.parametrize("path", [L.NB_CACHE_TCGEN05, L.NB_CACHE_MMA_SYNC])
 @pytest.mark.parametrize("n", [128, 2000])
-def test_gradient_matches_reference(n):
-    c = RadianceCache(seed=11)
+def test_gradient_matches_reference(n, path):
+    """Training gradients of both tensor-core paths (tcgen05 GEMMs with tensor-memory
+    accumulators, and mma.sync) against the CPU reference, on full and partial 128-row groups."""
+    c = RadianceCache(seed=11, tensor_path=path)
     w = c.get_weights()
     x, y = batch(n, 2)
     g = torch.zeros(N_PARAMS, device="cuda")
@@ -88,9 +91,10 @@ def test_gradient_matches_reference(n):
     assert np.all(g[R.LIVE_END:] == 0.0)
 
 
-def test_adam_step_matches_reference():
+@pytest.mark.parametrize("path", [L.NB_CACHE_TCGEN05, L.NB_CACHE_MMA_SYNC])
+def test_adam_step_matches_reference(path):
     cfg = dict(learning_rate=1e-2, beta1=0.9, beta2=0.99, epsilon=1e-8)
-    c = RadianceCache(seed=3, **cfg)
+    c = RadianceCache(seed=3, tensor_path=path, **cfg)
     w0 = c.get_weights()
     x, y = batch(1024, 4)
     g = torch.zeros(N_PARAMS, device="cuda")
