@@ -48,10 +48,10 @@ if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
 METRIC = "Mrays/s (primary + extension rays), 1920x1080 64spp 8 bounces"
-# DRAM bytes (read + write) per traversal query of k_trace_wave, from one ncu capture of the
-# same scene at 480x270, 4 spp (bounce-0 launch: 518,400 rays, 74.1 MB read + 6.0 MB
-# written); the roofline scales it to a full launch by the launch's rays
-TRACE_DRAM_BYTES_PER_RAY = 154.6
+# DRAM bytes (read + write) per traversal query of k_trace_wave over all bounces of a frame,
+# from one ncu capture of the same scene at 480x270, 64 spp (nine launches, 12,435,256 rays,
+# 1,208.7 MB read + 233.4 MB written); the roofline scales it to a launch by the launch's rays
+TRACE_DRAM_BYTES_PER_RAY = 116.0
 UNIT = "Mrays/s"
 WORKLOAD = "instanced 16 meshes / 1024 instances, 1920x1080, 64 spp, 8 bounces, equirect sky"
 # bytes the device layout fetches per unit of traversal work (nb_trace_counters): an 8-wide
@@ -88,6 +88,9 @@ def parse():
                    help="instead of the benchmark line, measure the other workloads (spheres 256x256 16 spp, "
                         "1M-triangle soup traversal) on GPU and CPU and print them as one JSON line")
     p.add_argument("--cache-frames", type=int, default=300, help="1-spp frames of online training on the camera path")
+    p.add_argument("--train-bench", action="store_true",
+                   help="instead of the benchmark line, time radiance-cache Adam steps of 16,384 seeded rows on both "
+                        "tensor-core paths (tcgen05 and mma.sync) and print them as one JSON line")
     return p.parse_args()
 
 
@@ -653,7 +656,8 @@ def trace_roofline(pt, scene, cam, env, desc, kt, steps, rays_per_step, sh, of):
             "counted_rays_per_step": int(counted_rays),
             "device_work_per_ray": {"bounce_0": per_ray(c[:1]), "bounces_1_plus": per_ray(c[1:])},
             "rays_per_bounce": [x["rays"] for x in c],
-            "traffic_note": "ncu dram bytes per ray of the 480x270 small-case capture x rays per launch",
+            "traffic_note": "ncu dram bytes per ray of all trace launches of the 480x270 64-spp small case "
+                            "(profiles/k_trace_wave__instanced_480x270_64spp.md) x rays per launch",
             "note": "achieved = bytes the 8-wide device layout fetches (instrumented counters of one extra "
                     "frame) / timed trace launch time, against the HBM copy peak; mostly L1/L2 hits, so the "
                     "kernel is bound by dependent-load latency and SIMT divergence, not by DRAM bandwidth"}
@@ -665,6 +669,34 @@ def trace_roofline(pt, scene, cam, env, desc, kt, steps, rays_per_step, sh, of):
             "note": "the reference's binary-BVH work per query (32 B per box test, 48 per triangle, 128 per "
                     "instance), counted by the oracle on the CPU sample: the work the device layout replaces"}
     return line
+
+
+def train_bench(args, rows=16384, warm=10, steps=100):
+    """Radiance-cache training on its own: Adam steps over `rows` seeded encoded rows (targets a
+    smooth function the network can fit), per tensor-core path; CUDA-event time per step
+    (each step returns its loss to the host, so the time includes that synchronisation)."""
+    import torch
+    import nbounce_gb300 as nb
+    from nbounce_gb300 import _lib as L
+    rng = np.random.default_rng(0)
+    x = rng.uniform(-1.0, 1.0, (rows, 64)).astype(np.float32)
+    x[:, 62], x[:, 63] = 1.0, 0.0
+    y = (0.5 + 0.4 * np.sin(x[:, :3] * 2.0 + x[:, 3:6])).astype(np.float32)
+    X, Y = torch.from_numpy(x).cuda(), torch.from_numpy(y).cuda()
+    out = {"rows_per_step": rows, "steps": steps, "flop_per_step": rows * MLP_FLOP_PER_RECORD}
+    for name, tp in (("tcgen05", L.NB_CACHE_TCGEN05), ("mma_sync", L.NB_CACHE_MMA_SYNC)):
+        c = nb.RadianceCache(seed=9, learning_rate=5e-3, tensor_path=tp)
+        for _ in range(warm):
+            c.train_step(X, Y, rows)
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record()
+        losses = [c.train_step(X, Y, rows) for _ in range(steps)]
+        b.record()
+        b.synchronize()
+        out[name] = {"ms_per_step": round(a.elapsed_time(b) / steps, 4), "final_loss": round(losses[-1], 6)}
+        c.close()
+    return out
 
 
 def run_ours(args):
@@ -832,6 +864,8 @@ def main():
     args.serving_loads = [(float(a), int(b)) for a, b in (x.split(":") for x in args.serving_loads.split(","))]
     if args.all_configs:
         line = configs_report(args)
+    elif args.train_bench:
+        line = train_bench(args)
     else:
         line = run_reference(args) if args.impl == "reference" else run_ours(args)
     if line is not None:
