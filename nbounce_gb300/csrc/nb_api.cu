@@ -664,6 +664,7 @@ static int render_samples(nb_pathtracer* pt, const nb_scene* scene, const nb_cam
     const uint32_t B = pt->globals.bounces;
     const bool nee = (pt->sampling & NB_SAMPLE_ENV_NEE) != 0 && !pt->cache;
     jp.flags = nee ? kJobEnvNee : 0u;
+    wt.flags = (nee || pt->cache) ? kWaveZeroRadiance : 0u;  // their shading adds to radiance
     if (nee) {
       if ((rc = ensure_shadow(pt, npix * S))) return rc;
       NB_CUDA(cudaMemsetAsync(pt->sq.counts, 0, 2 * kMaxBounceSlots * sizeof(uint32_t), st), "cudaMemsetAsync");

@@ -520,11 +520,12 @@ __global__ void __launch_bounds__(256) k_raygen(PathBatch pb, const WaveTables w
     generate_ray(x, y, jp.width, jp.height, jx, jy, jp.c2w, &o, &d);
     pb.q_o[0][q] = make_float4(o.x, o.y, o.z, __uint_as_float(p));
     pb.q_d[0][q] = make_float4(d.x, d.y, d.z, __uint_as_float(jp.scene));
-    pb.q_t[0][q] = make_float4(1.0f, 1.0f, 1.0f, 0.0f);
-    // a segment's queue positions and path ids cover the same range, so zeroing by queue
-    // position clears every path's radiance with coalesced stores (by path id, the lanes of a
-    // warp would store 16 bytes each, npix apart)
-    pb.radiance[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+    // the camera ray's throughput is (1, 1, 1) with lobe density 0 (q_t.w): the shade kernels
+    // take it as such at bounce 0 instead of reading it from the queue.  A segment's queue
+    // positions and path ids cover the same range, so zeroing by queue position clears every
+    // path's radiance with coalesced stores (by path id, the lanes of a warp would store 16
+    // bytes each, npix apart)
+    if (wt.flags & nb::kWaveZeroRadiance) pb.radiance[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   }
 }
 
@@ -1031,7 +1032,8 @@ __global__ void __launch_bounds__(kShadeThreads, 1) k_shade(PathBatch pb, const 
     bool cont = false;
     float4 next_o = make_float4(0.f, 0.f, 0.f, 0.f), next_d = next_o, next_t = next_o;
     if (i < n) {
-      const float4 O = in_o[i], D = in_d[i], Tq = in_t[i], H = pb.hits[i];
+      const float4 O = in_o[i], D = in_d[i], H = pb.hits[i];
+      const float4 Tq = bounce == 0 ? make_float4(1.0f, 1.0f, 1.0f, 0.0f) : in_t[i];
       const uint32_t id = __float_as_uint(O.w);
       const Segment sg = segs[find_segment<false>(segs, wt.n_segs, id)];
       const JobParams& jp = wt.jobs[sg.job];
@@ -1062,6 +1064,8 @@ __global__ void __launch_bounds__(kShadeThreads, 1) k_shade(PathBatch pb, const 
             next_o = make_float4(hs.pos.x, hs.pos.y, hs.pos.z, O.w);
             next_d = make_float4(bs.wi.x, bs.wi.y, bs.wi.z, D.w);
             next_t = make_float4(T.x, T.y, T.z, 0.0f);
+          } else {
+            pb.radiance[id] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);  // ends without radiance
           }
         }
       }
@@ -1137,7 +1141,8 @@ __global__ void __launch_bounds__(kShadeExtThreads) k_shade_cache(PathBatch pb, 
     V3 Tq3{0.0f, 0.0f, 0.0f};
     uint32_t slot = ~0u;
     if (i < n) {
-      const float4 O = in_o[i], D = in_d[i], Tq = in_t[i], H = pb.hits[i];
+      const float4 O = in_o[i], D = in_d[i], H = pb.hits[i];
+      const float4 Tq = bounce == 0 ? make_float4(1.0f, 1.0f, 1.0f, 0.0f) : in_t[i];
       const uint32_t id = __float_as_uint(O.w);
       const Segment sg = segs[find_segment<false>(segs, wt.n_segs, id)];
       const JobParams& jp = wt.jobs[sg.job];
@@ -1340,7 +1345,8 @@ __global__ void __launch_bounds__(kShadeExtThreads) k_shade_nee(PathBatch pb, co
     float4 next_o = make_float4(0.f, 0.f, 0.f, 0.f), next_d = next_o, next_t = next_o;
     float4 sh_o = next_o, sh_d = next_o, sh_c = next_o;
     if (i < n) {
-      const float4 O = in_o[i], D = in_d[i], Tq = in_t[i], H = pb.hits[i];
+      const float4 O = in_o[i], D = in_d[i], H = pb.hits[i];
+      const float4 Tq = bounce == 0 ? make_float4(1.0f, 1.0f, 1.0f, 0.0f) : in_t[i];
       const uint32_t id = __float_as_uint(O.w);
       const Segment sg = segs[find_segment<false>(segs, wt.n_segs, id)];
       const JobParams& jp = wt.jobs[sg.job];

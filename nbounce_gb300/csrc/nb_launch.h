@@ -40,9 +40,14 @@ struct Segment {
 };
 
 // Passed by value to the wave kernels (well under the 32 KB parameter limit).
+// flags: kWaveZeroRadiance - raygen zeroes every path's radiance, for waves whose shading adds
+// to it (environment NEE, radiance cache); with the reference estimator every path's radiance
+// is written once, where the path ends (k_shade), and raygen leaves it alone.
+constexpr uint32_t kWaveZeroRadiance = 1u << 0;
 struct WaveTables {
   uint32_t n_segs, n_jobs, n_scenes, n_paths, n_pix;
-  uint32_t pad[3];
+  uint32_t flags;
+  uint32_t pad[2];
   Segment segs[kMaxWaveSegments];
   JobParams jobs[kMaxWaveJobs];
   nbd::DevScene scenes[kMaxWaveScenes];

@@ -323,6 +323,7 @@ struct nb_server {
   cudaError_t launch_wave(uint32_t max_bounces, bool single_scene, bool nee) {
     PathBatch p = pb;
     cudaError_t e = cudaSuccess;
+    wt->flags = nee ? kWaveZeroRadiance : 0u;  // NEE shading adds to radiance
     if (nee) e = cudaMemsetAsync(sq.counts, 0, 2 * kMaxBounceSlots * sizeof(uint32_t), stream);
     if (e == cudaSuccess) e = launch_raygen(p, *wt, sms, stream);
     for (uint32_t b = 0; b <= max_bounces && e == cudaSuccess; ++b) {
@@ -351,6 +352,7 @@ struct nb_server {
   int launch_cache_wave(nb_cache* c, const CacheWave& cw, uint32_t max_bounces) {
     int rc = NB_OK;
     PathBatch p = pb;
+    wt->flags = kWaveZeroRadiance;  // cache lookups add to radiance
     cudaError_t e = launch_raygen(p, *wt, sms, stream);
     for (uint32_t b = 0; b <= max_bounces && e == cudaSuccess; ++b) {
       e = launch_trace_wave(p, *wt, true, b, d_rays, sms, stream);

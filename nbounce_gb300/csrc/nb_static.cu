@@ -122,6 +122,7 @@ extern "C" int nb_render_static(const nb_scene* scene, const nb_env* env, const 
 
   WaveTables& wt = g_tables;
   wt.n_jobs = wt.n_scenes = wt.n_segs = 1;
+  wt.flags = 0u;  // reference estimator: every path's radiance is written where it ends
   wt.scenes[0] = scene->dev;
   JobParams& jp = wt.jobs[0];
   std::memcpy(jp.c2w, camera->clip_to_world, sizeof(jp.c2w));
