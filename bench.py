@@ -50,8 +50,8 @@ if ROOT not in sys.path:
 METRIC = "Mrays/s (primary + extension rays), 1920x1080 64spp 8 bounces"
 # DRAM bytes (read + write) per traversal query of k_trace_wave over all bounces of a frame,
 # from one ncu capture of the same scene at 480x270, 64 spp (nine launches, 12,435,256 rays,
-# 1,208.7 MB read + 233.4 MB written); the roofline scales it to a launch by the launch's rays
-TRACE_DRAM_BYTES_PER_RAY = 116.0
+# 1,233.5 MB read + 238.2 MB written); the roofline scales it to a launch by the launch's rays
+TRACE_DRAM_BYTES_PER_RAY = 118.3
 UNIT = "Mrays/s"
 WORKLOAD = "instanced 16 meshes / 1024 instances, 1920x1080, 64 spp, 8 bounces, equirect sky"
 # bytes the device layout fetches per unit of traversal work (nb_trace_counters): an 8-wide
