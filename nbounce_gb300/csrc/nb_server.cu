@@ -151,7 +151,9 @@ struct nb_server {
   template <class Pick>
   void fail_jobs_locked(Pick pick, int status) {
     auto doomed = [&](Job* j) { return j->state != Job::kDone && pick(j); };
+    uint32_t n_failed = 0;
     auto count = [&] {
+      ++n_failed;
       ++jobs_failed;
       if (status == NB_ERR_CANCELLED) ++jobs_cancelled;
       if (status == NB_ERR_EXPIRED) ++jobs_expired;
@@ -172,6 +174,7 @@ struct nb_server {
       j->t_finish = now_ms();
       count();
     }
+    if (n_failed == 0) return;  // nothing changed: no erase, no wake-up (the deadline check runs every turn)
     active.erase(std::remove_if(active.begin(), active.end(), [](Job* j) { return j->state == Job::kDone; }),
                  active.end());
     cv_done.notify_all();
