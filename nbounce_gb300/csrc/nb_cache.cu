@@ -387,6 +387,20 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float (&v)[16]) {
   for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
 }
 
+// 64 consecutive FP32 accumulator columns of this thread's TMEM lane: one load, one wait
+// (four 16-column loads each waited for would take four round trips to tensor memory)
+__device__ __forceinline__ void tc_ld64(uint32_t taddr, float (&v)[64]) {
+  uint32_t r[64];
+  __syncwarp();  // warp-collective
+  asm volatile("tcgen05.ld.sync.aligned.32x32b.x64.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, %17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32, %33, %34, %35, %36, %37, %38, %39, %40, %41, %42, %43, %44, %45, %46, %47, %48, %49, %50, %51, %52, %53, %54, %55, %56, %57, %58, %59, %60, %61, %62, %63}, [%64];\n\t"
+               "tcgen05.wait::ld.sync.aligned;\n"
+               : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15]), "=r"(r[16]), "=r"(r[17]), "=r"(r[18]), "=r"(r[19]), "=r"(r[20]), "=r"(r[21]), "=r"(r[22]), "=r"(r[23]), "=r"(r[24]), "=r"(r[25]), "=r"(r[26]), "=r"(r[27]), "=r"(r[28]), "=r"(r[29]), "=r"(r[30]), "=r"(r[31]), "=r"(r[32]), "=r"(r[33]), "=r"(r[34]), "=r"(r[35]), "=r"(r[36]), "=r"(r[37]), "=r"(r[38]), "=r"(r[39]), "=r"(r[40]), "=r"(r[41]), "=r"(r[42]), "=r"(r[43]), "=r"(r[44]), "=r"(r[45]), "=r"(r[46]), "=r"(r[47]), "=r"(r[48]), "=r"(r[49]), "=r"(r[50]), "=r"(r[51]), "=r"(r[52]), "=r"(r[53]), "=r"(r[54]), "=r"(r[55]), "=r"(r[56]), "=r"(r[57]), "=r"(r[58]), "=r"(r[59]), "=r"(r[60]), "=r"(r[61]), "=r"(r[62]), "=r"(r[63])
+               : "r"(taddr)
+               : "memory");
+#pragma unroll
+  for (int i = 0; i < 64; ++i) v[i] = __uint_as_float(r[i]);
+}
+
 // kQueries: the rows are a wave's cache queries (encoded here; results go to radiance / tail);
 // else rows of encoded inputs X (bf16 [n][64]) with results in out[n][3].
 template <bool kQueries>
@@ -505,17 +519,13 @@ __global__ void __launch_bounds__(kTcThreads, 2) k_cache_infer_tc(const bf16* __
         const uint32_t t_row = tmem + 64u * j + lane_base;
         if (l < 5) {
           unsigned char* a = act + j * kTcActBytes;  // its MMA is complete: overwrite in place
+          float v[64];
+          tc_ld64(t_row, v);
 #pragma unroll
-          for (int c4 = 0; c4 < 4; ++c4) {
-            float v[16];
-            tc_ld16(t_row + 16u * c4, v);
-            *reinterpret_cast<uint4*>(a + canon_off(tid, 16u * c4)) =
-                make_uint4(pack2(relu(v[0]), relu(v[1])), pack2(relu(v[2]), relu(v[3])),
-                           pack2(relu(v[4]), relu(v[5])), pack2(relu(v[6]), relu(v[7])));
-            *reinterpret_cast<uint4*>(a + canon_off(tid, 16u * c4 + 8u)) =
-                make_uint4(pack2(relu(v[8]), relu(v[9])), pack2(relu(v[10]), relu(v[11])),
-                           pack2(relu(v[12]), relu(v[13])), pack2(relu(v[14]), relu(v[15])));
-          }
+          for (int c = 0; c < 8; ++c)
+            *reinterpret_cast<uint4*>(a + canon_off(tid, 8u * c)) =
+                make_uint4(pack2(relu(v[8 * c]), relu(v[8 * c + 1])), pack2(relu(v[8 * c + 2]), relu(v[8 * c + 3])),
+                           pack2(relu(v[8 * c + 4]), relu(v[8 * c + 5])), pack2(relu(v[8 * c + 6]), relu(v[8 * c + 7])));
           fence_async_smem();
         } else {
           // every lane of every warp runs the (warp-collective) accumulator load; only rows
@@ -927,17 +937,13 @@ __global__ void __launch_bounds__(128, 1) k_cache_grad_tc(const unsigned char* _
     const bool ok = wait_all();
     if (l < 5) {
       unsigned char* h = H + (l + 1) * kTrAct;
+      float v[64];
+      tc_ld64(d_layer + lane_base, v);
 #pragma unroll
-      for (uint32_t c4 = 0; c4 < 4; ++c4) {
-        float v[16];
-        tc_ld16(d_layer + lane_base + 16u * c4, v);
-        *reinterpret_cast<uint4*>(h + canon_off(tid, 16u * c4)) =
-            make_uint4(pack2(relu(v[0]), relu(v[1])), pack2(relu(v[2]), relu(v[3])), pack2(relu(v[4]), relu(v[5])),
-                       pack2(relu(v[6]), relu(v[7])));
-        *reinterpret_cast<uint4*>(h + canon_off(tid, 16u * c4 + 8u)) =
-            make_uint4(pack2(relu(v[8]), relu(v[9])), pack2(relu(v[10]), relu(v[11])),
-                       pack2(relu(v[12]), relu(v[13])), pack2(relu(v[14]), relu(v[15])));
-      }
+      for (uint32_t c = 0; c < 8; ++c)
+        *reinterpret_cast<uint4*>(h + canon_off(tid, 8u * c)) =
+            make_uint4(pack2(relu(v[8 * c]), relu(v[8 * c + 1])), pack2(relu(v[8 * c + 2]), relu(v[8 * c + 3])),
+                       pack2(relu(v[8 * c + 4]), relu(v[8 * c + 5])), pack2(relu(v[8 * c + 6]), relu(v[8 * c + 7])));
     } else {
       // output layer: dL/dp = 2 (p - y) / (p^2 + 0.01) with the denominator held constant
       float v[16];
@@ -999,19 +1005,15 @@ __global__ void __launch_bounds__(128, 1) k_cache_grad_tc(const unsigned char* _
     if (l >= 1) {
       // dZ_l = dH_l where H_l > 0 (BF16 activation), written over dZ (its MMAs are complete)
       const unsigned char* hl = H + l * kTrAct;
+      float v[64];
+      tc_ld64(d_layer + lane_base, v);
 #pragma unroll
-      for (uint32_t c4 = 0; c4 < 4; ++c4) {
-        float v[16];
-        tc_ld16(d_layer + lane_base + 16u * c4, v);
-        const uint4 m0 = *reinterpret_cast<const uint4*>(hl + canon_off(tid, 16u * c4));
-        const uint4 m1 = *reinterpret_cast<const uint4*>(hl + canon_off(tid, 16u * c4 + 8u));
-        *reinterpret_cast<uint4*>(dZ + canon_off(tid, 16u * c4)) =
-            make_uint4(pack2(gate_lo(v[0], m0.x), gate_hi(v[1], m0.x)), pack2(gate_lo(v[2], m0.y), gate_hi(v[3], m0.y)),
-                       pack2(gate_lo(v[4], m0.z), gate_hi(v[5], m0.z)), pack2(gate_lo(v[6], m0.w), gate_hi(v[7], m0.w)));
-        *reinterpret_cast<uint4*>(dZ + canon_off(tid, 16u * c4 + 8u)) =
-            make_uint4(pack2(gate_lo(v[8], m1.x), gate_hi(v[9], m1.x)), pack2(gate_lo(v[10], m1.y), gate_hi(v[11], m1.y)),
-                       pack2(gate_lo(v[12], m1.z), gate_hi(v[13], m1.z)),
-                       pack2(gate_lo(v[14], m1.w), gate_hi(v[15], m1.w)));
+      for (uint32_t c = 0; c < 8; ++c) {
+        const uint4 m = *reinterpret_cast<const uint4*>(hl + canon_off(tid, 8u * c));
+        const float* x = v + 8 * c;
+        *reinterpret_cast<uint4*>(dZ + canon_off(tid, 8u * c)) =
+            make_uint4(pack2(gate_lo(x[0], m.x), gate_hi(x[1], m.x)), pack2(gate_lo(x[2], m.y), gate_hi(x[3], m.y)),
+                       pack2(gate_lo(x[4], m.z), gate_hi(x[5], m.z)), pack2(gate_lo(x[6], m.w), gate_hi(x[7], m.w)));
       }
     }
     publish(!ok);
@@ -1022,15 +1024,12 @@ __global__ void __launch_bounds__(128, 1) k_cache_grad_tc(const unsigned char* _
       const uint32_t outs = l == 5 ? 16u : 64u;
       const uint32_t d_w = tmem + 64u + 64u * (uint32_t)(l & 1);
       float* d = dw + (size_t)l * 4096u + (size_t)tid * 64u;
+      float v[64];
+      tc_ld64(d_w + lane_base, v);
+      if (tid < outs) {
 #pragma unroll
-      for (uint32_t c4 = 0; c4 < 4; ++c4) {
-        float v[16];
-        tc_ld16(d_w + lane_base + 16u * c4, v);
-        if (tid < outs) {
-#pragma unroll
-          for (int q = 0; q < 4; ++q)
-            *reinterpret_cast<float4*>(d + 16u * c4 + 4u * q) = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
-        }
+        for (int q = 0; q < 16; ++q)
+          *reinterpret_cast<float4*>(d + 4u * q) = make_float4(v[4 * q], v[4 * q + 1], v[4 * q + 2], v[4 * q + 3]);
       }
     }
     // the next round's epilogue overwrites dZ only after its wait, i.e. after these loads
