@@ -1,5 +1,5 @@
-// CPU oracle of BC6H block decoding (TEST INFRASTRUCTURE ONLY: loaded by tests/ as the checker
-// of the library's device decoder; the product never links or calls it).
+// CPU oracle of BC6H block decoding (TEST INFRASTRUCTURE ONLY: loaded by tests/ to check the
+// library's device decoder against; the product never links or calls it).
 //
 // The reference samples its environment from a BC6H_UF16 cube texture (texture.rs:89-94,
 // pathtracing.wgsl:168) and leaves the decoding to the graphics hardware, so the reference
