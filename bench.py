@@ -710,10 +710,13 @@ def run_ours(args):
     from nbounce_gb300 import replicas
 
     rank, world, local = dist_env()
-    if world > 1:
-        torch.cuda.set_device(local)
-        torch.distributed.init_process_group("nccl", device_id=torch.device("cuda", local))
     torch.cuda.set_device(local)
+    grouped = world > 1 or args.shard_frame  # --shard-frame merges over NCCL even with one rank
+    if grouped:
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        os.environ.setdefault("MASTER_PORT", str(free_port()))
+        torch.distributed.init_process_group("nccl", rank=rank, world_size=world,
+                                             device_id=torch.device("cuda", local))
     dev = torch.device("cuda", local)
     desc = build_workload(args)
     t0 = time.perf_counter()
@@ -728,7 +731,7 @@ def run_ours(args):
         pt.set_sampling(env_nee=True)
     stream = torch.cuda.current_stream(dev)
     sh = stream.cuda_stream
-    shard = args.shard_frame and world > 1
+    shard = args.shard_frame
     first, count = replicas.shard_samples(desc.spp, rank, world) if shard else (1, desc.spp)
     ptr, w, h = pt.output_texture()
     image = torch.as_tensor(_DeviceView(ptr, (h, w, 4)), device=dev)
@@ -800,7 +803,7 @@ def run_ours(args):
     value = total_rays / (t_max / 1e3) / 1e6
     e2e_value = total_rays / e2e_max / 1e6
     if rank != 0:
-        if world > 1:
+        if grouped:
             torch.distributed.destroy_process_group()
         return None
     launches_per_step = sum(kt[k] for k in ("raygen_launches", "trace_launches", "shade_launches",
@@ -831,7 +834,7 @@ def run_ours(args):
         line["serving"] = serving_report(args)
     if not args.no_cache and world == 1:
         line["cache"] = cache_report(args, desc, scene, env, stream)
-    if world > 1:
+    if grouped:
         torch.distributed.destroy_process_group()
     return line
 
