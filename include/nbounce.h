@@ -339,8 +339,7 @@ int nb_scene_status(const nb_scene* scene, uint32_t* status, void* stream);
  * lives in one static device array of 34.9 MB reserved per GPU at library load; images above
  * 262,144 pixels are rejected with NB_ERR_INVALID_ARG.  The first call on a device does a
  * one-time set-up there (looks up that array's device address and uploads the Sobol table
- * into it, synchronously), so make that first call before any stream capture begins.  Every
- * call checks that the array still holds the table and repeats the set-up if not (after a
+ * into it, synchronously).  Every call checks that the array still holds the table and repeats the set-up if not (after a
  * device reset the module is reloaded and its arrays start zeroed); scenes and environments
  * do not survive a device reset and must be created again.  Calls share the array (it keeps
  * the last call's contents); calls that overlap on the GPU race on it.  Synchronises stream.

@@ -11,7 +11,7 @@
 // (512 x 512); samples run in waves of floor(262,144 / pixels) samples.  The array is 34.9 MB.
 // Its device address is looked up once per device, with that device current, on the first
 // call there (cudaGetSymbolAddress; the same call uploads the Sobol table and a marker word
-// behind it) - make that first call before any stream capture begins.  Every later call looks
+// behind it).  Every later call looks
 // the address up again and reads the marker back; if either changed (a device reset reloads
 // the module, whose arrays then start zeroed) it repeats the set-up.  Every call shares the
 // array and it keeps the last call's contents; the kernels reset what must start at zero.
