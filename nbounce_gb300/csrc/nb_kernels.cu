@@ -106,6 +106,35 @@ __device__ __forceinline__ void trace_begin(TraceState& t, uint2* stack, const D
   t.iter = 0;
 }
 
+// Where trace_step reads the world ray when it enters or leaves an instance: the traversal
+// state's registers (WorldRegs), or a per-warp array in shared memory (WorldShared,
+// component-major so that the 32 lanes' loads hit distinct banks), which keeps six registers
+// free in the kernels whose register budget is tightest.
+struct WorldRegs {
+  const TraceState& t;
+  __device__ __forceinline__ V3 o() const { return t.wo; }
+  __device__ __forceinline__ V3 d() const { return t.wd; }
+};
+constexpr int kWorldFloats = 6 * 32;  // one warp's world rays: ox, oy, oz, dx, dy, dz x 32 lanes
+constexpr int kTraceWarps = 4;  // every traversal kernel runs blocks of 128 threads
+constexpr int kTraceThreads = 32 * kTraceWarps;
+struct WorldShared {
+  float* w;
+  __device__ __forceinline__ V3 o() const {
+    const uint32_t l = threadIdx.x & 31u;
+    return V3{w[l], w[32 + l], w[64 + l]};
+  }
+  __device__ __forceinline__ V3 d() const {
+    const uint32_t l = threadIdx.x & 31u;
+    return V3{w[96 + l], w[128 + l], w[160 + l]};
+  }
+  __device__ __forceinline__ void set(V3 o, V3 d) const {
+    const uint32_t l = threadIdx.x & 31u;
+    w[l] = o.x; w[32 + l] = o.y; w[64 + l] = o.z;
+    w[96 + l] = d.x; w[128 + l] = d.y; w[160 + l] = d.z;
+  }
+};
+
 // Work counters of the instrumented traversal (kCount instantiations only): what the device
 // layout fetches per ray - 80-byte wide nodes of the TLAS and the BLASes, 48-byte triangle
 // records, 64-byte instance records - and the 8-byte stack entries pushed (each later popped).
@@ -115,15 +144,15 @@ struct TraceCount {
 
 // One traversal step: pop the next entry when no node is pending, then test one 8-wide node
 // and its leaf triangles.  Returns false once the ray is finished (stack empty, an any-hit
-// found, or the iteration cap reached).
-template <bool kAny, bool kCount = false>
-__device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const DevScene& s, TraceCount* cnt = nullptr) {
+// found, or the iteration cap reached).  wr gives the world ray (WorldRegs / WorldShared).
+template <bool kAny, bool kCount, class World>
+__device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const DevScene& s, TraceCount* cnt,
+                                           const World& wr) {
   if (t.iter > kIterationCap) {
     t.status |= kStatusIterationCap;
     return false;
   }
   ++t.iter;
-  const V3 wo = t.wo, wd = t.wd;
   V3 &ro = t.ro, &rd = t.rd, &rinv = t.rinv;
   float& h_t = t.t_hit;
   int &sp = t.sp, &blas_base = t.blas_base;
@@ -134,7 +163,8 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
     for (;;) {
       if (in_blas && sp == blas_base) {  // BLAS finished: back to the world ray
         in_blas = false;
-        ro = wo; rd = wd;
+        const V3 wd = wr.d();
+        ro = wr.o(); rd = wd;
         rinv = V3{safe_rcp(wd.x), safe_rcp(wd.y), safe_rcp(wd.z)};
       }
       if (sp == 0) {
@@ -149,6 +179,7 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
         if (kCount) ++cnt->insts;
         const float4* it = s.inst_trace + 4 * (size_t)(e.x & ~kInstanceBit);
         const float4 r0 = ld4(it), r1 = ld4(it + 1), r2 = ld4(it + 2), r3 = ld4(it + 3);
+        const V3 wo = wr.o(), wd = wr.d();
         ro = V3{r0.x * wo.x + r0.y * wo.y + r0.z * wo.z + r0.w * 1.0f,
                 r1.x * wo.x + r1.y * wo.y + r1.z * wo.z + r1.w * 1.0f,
                 r2.x * wo.x + r2.y * wo.y + r2.z * wo.z + r2.w * 1.0f};
@@ -177,6 +208,17 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
   const float ay = __uint_as_float(((eb >> 8) & 0xFFu) << 23) * rinv.y;
   const float az = __uint_as_float(((eb >> 16) & 0xFFu) << 23) * rinv.z;
   const float bx = (q0.x - ro.x) * rinv.x, by = (q0.y - ro.y) * rinv.y, bz = (q0.z - ro.z) * rinv.z;
+  // A plane byte q is read as the float F = 2^15 + q (one byte permute: bytes 0, q, 0, 0x47)
+  // and its distance taken as fma(F, a, b - 2^15 a), one rounding more than fma(q, a, b): the
+  // folded constant differs from b - 2^15 a by at most 2^-24 (|b| + 2^15 |a|), so each plane's
+  // distance lies within 2^-24 (3 |b| + (2^15 + 510) |a|) of fma(q, a, b).  Near-plane
+  // constants are lowered and far-plane constants raised by more than twice that (|a| / 128 +
+  // |b| / 2^20), so the test accepts every ray the unfolded one accepts.
+  const float dx = fmaf(fabsf(ax), 0.0078125f, fabsf(bx) * 9.5367431640625e-7f);
+  const float dy = fmaf(fabsf(ay), 0.0078125f, fabsf(by) * 9.5367431640625e-7f);
+  const float dz = fmaf(fabsf(az), 0.0078125f, fabsf(bz) * 9.5367431640625e-7f);
+  const float cx = fmaf(-32768.0f, ax, bx), cy = fmaf(-32768.0f, ay, by), cz = fmaf(-32768.0f, az, bz);
+  const float cnx = cx - dx, cfx = cx + dx, cny = cy - dy, cfy = cy + dy, cnz = cz - dz, cfz = cz + dz;
   const uint32_t child_base = f2u(q1.x), prim_base = f2u(q1.y);
   const uint32_t m0 = f2u(q1.z), m1 = f2u(q1.w);
   // near/far planes per axis by the sign of the direction: the near plane of a child is its
@@ -194,17 +236,17 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
   uint32_t leaf_mask = 0, n_push = 0;
 #pragma unroll
   for (int k = 0; k < 8; ++k) {
-    // byte k as a float: bits 0x4B0000bb are 2^23 + bb, so subtracting 2^23 is exact
-    const uint32_t sel = 0x7540u + (uint32_t)(k & 3);
+    // byte k of the plane words as the float 2^15 + q: bits 0x4700qq00
+    const uint32_t sel = 0x7404u + ((uint32_t)(k & 3) << 4);
     const uint32_t meta = __byte_perm(k < 4 ? m0 : m1, 0u, 0x4440u + (uint32_t)(k & 3));
-    const float nx = __uint_as_float(__byte_perm(k < 4 ? nx0 : nx1, 0x4B000000u, sel)) - 8388608.0f;
-    const float fx = __uint_as_float(__byte_perm(k < 4 ? fx0 : fx1, 0x4B000000u, sel)) - 8388608.0f;
-    const float ny = __uint_as_float(__byte_perm(k < 4 ? ny0 : ny1, 0x4B000000u, sel)) - 8388608.0f;
-    const float fy = __uint_as_float(__byte_perm(k < 4 ? fy0 : fy1, 0x4B000000u, sel)) - 8388608.0f;
-    const float nz = __uint_as_float(__byte_perm(k < 4 ? nz0 : nz1, 0x4B000000u, sel)) - 8388608.0f;
-    const float fz = __uint_as_float(__byte_perm(k < 4 ? fz0 : fz1, 0x4B000000u, sel)) - 8388608.0f;
-    const float tn = fmaxf(fmaxf(fmaf(nx, ax, bx), fmaf(ny, ay, by)), fmaf(nz, az, bz));
-    const float tf = fminf(fminf(fmaf(fx, ax, bx), fmaf(fy, ay, by)), fmaf(fz, az, bz)) * kFarSlack;
+    const float nx = __uint_as_float(__byte_perm(k < 4 ? nx0 : nx1, 0x47000000u, sel));
+    const float fx = __uint_as_float(__byte_perm(k < 4 ? fx0 : fx1, 0x47000000u, sel));
+    const float ny = __uint_as_float(__byte_perm(k < 4 ? ny0 : ny1, 0x47000000u, sel));
+    const float fy = __uint_as_float(__byte_perm(k < 4 ? fy0 : fy1, 0x47000000u, sel));
+    const float nz = __uint_as_float(__byte_perm(k < 4 ? nz0 : nz1, 0x47000000u, sel));
+    const float fz = __uint_as_float(__byte_perm(k < 4 ? fz0 : fz1, 0x47000000u, sel));
+    const float tn = fmaxf(fmaxf(fmaf(nx, ax, cnx), fmaf(ny, ay, cny)), fmaf(nz, az, cnz));
+    const float tf = fminf(fminf(fmaf(fx, ax, cfx), fmaf(fy, ay, cfy)), fmaf(fz, az, cfz)) * kFarSlack;
     const float lo = fmaxf(tn, 0.0f);
     const bool hit = meta != 0u && lo <= fminf(tf, t_below);
     key[k] = 0xFFFFFFFFu;
@@ -309,7 +351,7 @@ __device__ __forceinline__ uint32_t trace_ray(const DevScene& s, const V3 wo, co
   TraceState t;
   uint2 stack[kStackSize + 2];
   trace_begin(t, stack, s, wo, wd);
-  while (trace_step<kAny, kCount>(t, stack, s, cnt)) {
+  while (trace_step<kAny, kCount>(t, stack, s, cnt, WorldRegs{t})) {
   }
   const uint2 uv = stack[kHitSlot], ti = stack[kHitSlot + 1];
   h.t = t.t_hit;
@@ -324,15 +366,17 @@ __device__ __forceinline__ uint32_t trace_ray(const DevScene& s, const V3 wo, co
 // takes a new one once kRefillIdle lanes of the warp are idle (a whole idle warp always takes
 // 32), all of them with one atomic on *fetch.  load(r, o, d, sidx) reads ray r and its scene
 // index; scene(sidx) gives that scene; finish(r, t_hit, uv, tri_inst) consumes ray r's hit
-// record (t = kNoHit on a miss).  Every lane of the warp must call it.  Returns the status
-// bits its rays raised.  Used where the rays of a warp are incoherent (secondary and shadow
-// rays, caller rays): their traversal lengths differ widely, and without refill most lanes
-// would idle while the longest ray of each 32 finishes.  Refill changes only which lane traces
-// a ray, not its result.
+// record (t = kNoHit on a miss).  world is this warp's kWorldFloats floats of shared memory,
+// where the lanes' world rays are kept (WorldShared).  Every lane of the warp must call it.
+// Returns the status bits its rays raised.  Used where the rays of a warp are incoherent
+// (secondary and shadow rays, caller rays): their traversal lengths differ widely, and without
+// refill most lanes would idle while the longest ray of each 32 finishes.  Refill changes only
+// which lane traces a ray, not its result.
 constexpr uint32_t kRefillIdle = 8;
 template <bool kAny, bool kCount, class Load, class SceneOf, class Finish>
 __device__ __forceinline__ uint32_t trace_refill(uint32_t* fetch, uint32_t n, Load load, SceneOf scene, Finish finish,
-                                                 TraceCount* cnt) {
+                                                 TraceCount* cnt, float* world) {
+  const WorldShared wr{world};
   const uint32_t lane = threadIdx.x & 31u;
   TraceState t;
   uint2 stack[kStackSize + 2];
@@ -354,10 +398,11 @@ __device__ __forceinline__ uint32_t trace_refill(uint32_t* fetch, uint32_t n, Lo
           V3 o, d;
           load(r, o, d, sidx);
           trace_begin(t, stack, scene(sidx), o, d);
+          wr.set(o, d);
         }
       }
     }
-    if (my != kNone && !trace_step<kAny, kCount>(t, stack, scene(sidx), cnt)) {
+    if (my != kNone && !trace_step<kAny, kCount>(t, stack, scene(sidx), cnt, wr)) {
       finish(my, t.t_hit, stack[kHitSlot], stack[kHitSlot + 1]);
       st |= t.status;
       my = kNone;
@@ -372,14 +417,17 @@ __device__ __forceinline__ uint32_t trace_refill(uint32_t* fetch, uint32_t n, Lo
 // traversal-only query (nb_trace_rays)
 // ------------------------------------------------------------------------------------------
 // kRefill: lanes refill as they finish (trace_refill), for rays whose neighbours in the array
-// are unrelated; else each warp traces 32 consecutive rays to the end.
+// are unrelated; else each warp traces 32 consecutive rays to the end.  The refill and any-hit
+// instantiations fit 64 registers without spills and run 8 blocks per SM, closest hit without
+// refill 7 blocks at 72 registers.
 template <bool kAny, bool kRefill>
-__global__ void __launch_bounds__(128) k_trace_rays(DevScene s, const float4* __restrict__ rays, uint32_t n,
+__global__ void __launch_bounds__(kTraceThreads, kRefill || kAny ? 8 : 7) k_trace_rays(DevScene s, const float4* __restrict__ rays, uint32_t n,
                                                      float4* __restrict__ hits, uint32_t* __restrict__ inst,
                                                      uint32_t* __restrict__ fetch, uint32_t* __restrict__ status) {
   const int lane = threadIdx.x & 31;
   uint32_t st = 0;
   if (kRefill) {
+    __shared__ float world[kTraceWarps][kWorldFloats];
     st = trace_refill<kAny, false>(
         fetch, n,
         [&](uint32_t r, V3& o, V3& d, uint32_t& sidx) {
@@ -392,7 +440,7 @@ __global__ void __launch_bounds__(128) k_trace_rays(DevScene s, const float4* __
           hits[r] = make_float4(t_hit, __uint_as_float(uv.x), __uint_as_float(uv.y), __uint_as_float(ti.x));
           if (inst) inst[r] = ti.y;
         },
-        nullptr);
+        nullptr, world[threadIdx.x >> 5]);
   } else {
     while (true) {
       uint32_t base = 0;
@@ -549,7 +597,7 @@ __global__ void __launch_bounds__(256) k_raygen(PathBatch pb, const WaveTables w
 // blocks of 128 per SM instead of 7 at 72 (measured: secondary-ray traversal 2.6 ms faster per
 // frame; 6 blocks at 80 registers 5.2 ms slower, 9 blocks at 56 spills).
 template <bool kSingle, bool kCount, bool kRefill>
-__global__ void __launch_bounds__(128, kRefill ? 8 : 7) k_trace_wave(PathBatch pb, const WaveTables wt,
+__global__ void __launch_bounds__(kTraceThreads, kRefill ? 8 : 7) k_trace_wave(PathBatch pb, const WaveTables wt,
                                                                      uint32_t bounce,
                                                        unsigned long long* __restrict__ ray_total,
                                                        unsigned long long* __restrict__ counters) {
@@ -581,6 +629,7 @@ __global__ void __launch_bounds__(128, kRefill ? 8 : 7) k_trace_wave(PathBatch p
       }
     }
   } else {
+    __shared__ float world[kTraceWarps][kWorldFloats];
     const DevScene* sc = kSingle ? wt.scenes : scenes;
     st = trace_refill<false, kCount>(
         pb.fetch + bounce, n,
@@ -595,7 +644,7 @@ __global__ void __launch_bounds__(128, kRefill ? 8 : 7) k_trace_wave(PathBatch p
           pb.hits[r] = make_float4(t_hit, __uint_as_float(uv.x), __uint_as_float(uv.y), __uint_as_float(ti.x));
           pb.hit_inst[r] = ti.y;
         },
-        &cnt);
+        &cnt, world[threadIdx.x >> 5]);
   }
   if (st) atomicOr(pb.status, st);
   if (kCount) {
@@ -1435,11 +1484,12 @@ __global__ void __launch_bounds__(kShadeExtThreads) k_shade_nee(PathBatch pb, co
 // refill (trace_refill); unoccluded rays add their contribution to the path.  A path has at most one shadow ray per bounce, so
 // each radiance entry has one writer per launch.  .w of a shadow ray's direction is the index
 // of its scene in the wave.
-__global__ void __launch_bounds__(128, 8) k_trace_shadow(PathBatch pb, const WaveTables wt, const ShadowQueue sq,
+__global__ void __launch_bounds__(kTraceThreads, 8) k_trace_shadow(PathBatch pb, const WaveTables wt, const ShadowQueue sq,
                                                       uint32_t bounce) {
   __shared__ DevScene scenes[nb::kMaxWaveScenes];
   for (uint32_t i = threadIdx.x; i < wt.n_scenes; i += blockDim.x) scenes[i] = wt.scenes[i];
   __syncthreads();
+  __shared__ float world[kTraceWarps][kWorldFloats];
   const uint32_t n = sq.counts[bounce];
   const uint32_t st = trace_refill<true, false>(
       sq.fetch + bounce, n,
@@ -1457,7 +1507,7 @@ __global__ void __launch_bounds__(128, 8) k_trace_shadow(PathBatch pb, const Wav
           pb.radiance[id] = make_float4(rr.x + c.x, rr.y + c.y, rr.z + c.z, 0.0f);
         }
       },
-      nullptr);
+      nullptr, world[threadIdx.x >> 5]);
   if (st) atomicOr(pb.status, st);
 }
 
@@ -1511,8 +1561,8 @@ cudaError_t launch_trace_rays(const nbd::DevScene& s, const float* rays, uint32_
   if (n == 0) return cudaSuccess;
 #define NB_TRACE_RAYS(A, R)                                                                            \
   {                                                                                                    \
-    static const int g = blocks_for((const void*)nbd::k_trace_rays<A, R>, 128, sms);                  \
-    nbd::k_trace_rays<A, R><<<g, 128, 0, st>>>(s, (const float4*)rays, n, (float4*)hits, inst, fetch, status); \
+    static const int g = blocks_for((const void*)nbd::k_trace_rays<A, R>, nbd::kTraceThreads, sms);                  \
+    nbd::k_trace_rays<A, R><<<g, nbd::kTraceThreads, 0, st>>>(s, (const float4*)rays, n, (float4*)hits, inst, fetch, status); \
   }
   if (any) {
     if (refill) NB_TRACE_RAYS(true, true) else NB_TRACE_RAYS(true, false)
@@ -1535,8 +1585,8 @@ cudaError_t launch_trace_wave(const PathBatch& pb, const WaveTables& wt, bool si
   const bool refill = bounce >= 1;
 #define NB_TRACE_WAVE(S, C, R)                                                                \
   {                                                                                           \
-    static const int g = blocks_for((const void*)nbd::k_trace_wave<S, C, R>, 128, sms);       \
-    nbd::k_trace_wave<S, C, R><<<g, 128, 0, st>>>(pb, wt, bounce, ray_total, counters);      \
+    static const int g = blocks_for((const void*)nbd::k_trace_wave<S, C, R>, nbd::kTraceThreads, sms);       \
+    nbd::k_trace_wave<S, C, R><<<g, nbd::kTraceThreads, 0, st>>>(pb, wt, bounce, ray_total, counters);      \
   }
   if (counters) {
     if (single_scene) {
@@ -1575,8 +1625,8 @@ cudaError_t launch_shade_nee(const PathBatch& pb, const WaveTables& wt, const Sh
 
 cudaError_t launch_trace_shadow(const PathBatch& pb, const WaveTables& wt, const ShadowQueue& sq, uint32_t bounce,
                                 int sms, cudaStream_t st) {
-  static const int g = blocks_for((const void*)nbd::k_trace_shadow, 128, sms);
-  nbd::k_trace_shadow<<<g, 128, 0, st>>>(pb, wt, sq, bounce);
+  static const int g = blocks_for((const void*)nbd::k_trace_shadow, nbd::kTraceThreads, sms);
+  nbd::k_trace_shadow<<<g, nbd::kTraceThreads, 0, st>>>(pb, wt, sq, bounce);
   return cudaGetLastError();
 }
 
