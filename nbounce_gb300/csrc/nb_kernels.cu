@@ -47,9 +47,6 @@ using nb::WaveTables;
 constexpr int kStackSize = 64;
 constexpr uint32_t kIterationCap = 1u << 22;
 constexpr uint32_t kInstanceBit = 0x80000000u;
-// t-space slack of the quantised slab test: covers the rounding of the fused plane
-// evaluation so that a box never rejects a ray the exact reference box accepts
-constexpr float kFarSlack = 1.0000004f;
 
 __device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
 __device__ __forceinline__ uint32_t f2u(float x) { return __float_as_uint(x); }
@@ -211,9 +208,12 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
   // A plane byte q is read as the float F = 2^15 + q (one byte permute: bytes 0, q, 0, 0x47)
   // and its distance taken as fma(F, a, b - 2^15 a), one rounding more than fma(q, a, b): the
   // folded constant differs from b - 2^15 a by at most 2^-24 (|b| + 2^15 |a|), so each plane's
-  // distance lies within 2^-24 (3 |b| + (2^15 + 510) |a|) of fma(q, a, b).  Near-plane
-  // constants are lowered and far-plane constants raised by more than twice that (|a| / 128 +
-  // |b| / 2^20), so the test accepts every ray the unfolded one accepts.
+  // distance lies within e = 2^-24 (3 |b| + (2^15 + 510) |a|) of fma(q, a, b).  Near-plane
+  // constants are lowered and far-plane constants raised by d = |a| / 128 + |b| / 2^20 per
+  // axis.  d - e >= 7.7e-7 |b| + 0.0058 |a| >= 4e-7 (|b| + 255 |a|) >= 4e-7 |t| for every plane
+  // t = b + q a of the node: besides the fold, the margin covers the rounding of the plane
+  // evaluation against the exact reference box (a relative 4e-7 of the distance), so that a
+  // box never rejects a ray the reference box accepts.
   const float dx = fmaf(fabsf(ax), 0.0078125f, fabsf(bx) * 9.5367431640625e-7f);
   const float dy = fmaf(fabsf(ay), 0.0078125f, fabsf(by) * 9.5367431640625e-7f);
   const float dz = fmaf(fabsf(az), 0.0078125f, fabsf(bz) * 9.5367431640625e-7f);
@@ -246,7 +246,7 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
     const float nz = __uint_as_float(__byte_perm(k < 4 ? nz0 : nz1, 0x47000000u, sel));
     const float fz = __uint_as_float(__byte_perm(k < 4 ? fz0 : fz1, 0x47000000u, sel));
     const float tn = fmaxf(fmaxf(fmaf(nx, ax, cnx), fmaf(ny, ay, cny)), fmaf(nz, az, cnz));
-    const float tf = fminf(fminf(fmaf(fx, ax, cfx), fmaf(fy, ay, cfy)), fmaf(fz, az, cfz)) * kFarSlack;
+    const float tf = fminf(fminf(fmaf(fx, ax, cfx), fmaf(fy, ay, cfy)), fmaf(fz, az, cfz));
     const float lo = fmaxf(tn, 0.0f);
     const bool hit = meta != 0u && lo <= fminf(tf, t_below);
     key[k] = 0xFFFFFFFFu;
