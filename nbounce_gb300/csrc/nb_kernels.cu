@@ -882,12 +882,16 @@ __device__ __forceinline__ void append_init(uint32_t* sh) {
   for (uint32_t i = threadIdx.x; i < kDirBins; i += blockDim.x) sh[i] = 0u;
   __syncthreads();
 }
-// k_shade: 512 threads capped at 64 registers (2 blocks per SM) measured 1.3% faster than 256
-// threads at 68 registers (3 blocks); 1024 threads (1 block per SM, the same warps) another
-// 0.5%: the next bounce's rays are grouped by direction over twice as many survivors, which
-// saves more traversal than the block-wide barriers cost.  The NEE and cache shade kernels
-// (78 registers) stay at 256 threads, where that cap would spill
-constexpr int kShadeThreads = 1024;
+// k_shade: blocks of 256 threads at 64 registers, 4 per SM.  Each block bins its survivors
+// by direction, and the binning's two block-wide barriers stall only that block.  With one
+// 1024-thread block per SM (twice the survivors per bin of 512 threads, which once paid) every
+// barrier stalled the whole SM; since lanes refill during traversal, the larger bins save
+// little: benchmark frame 101.1 ms with 1024 threads, 100.4 with 512, 100.1 with 256 (shading
+// 9.6 -> 8.2 ms, traversal +0.3 ms); a warp-level append without binning: 100.4 (shading 7.4,
+// traversal +1.4).  The NEE and cache shade kernels (78 registers) run 256 threads without the
+// register cap, which would spill
+constexpr int kShadeThreads = 256;
+constexpr int kShadeBlocksPerSM = 4;
 constexpr int kShadeExtThreads = 256;
 __device__ __forceinline__ uint32_t block_append_binned(uint32_t* counter, bool active, float4 dir, uint32_t* sh) {
   uint32_t* cnt = sh;
@@ -1064,7 +1068,7 @@ __device__ __forceinline__ float rr_continue(uint32_t bounce, const JobParams& j
   return bounce < jp.rr_start ? 1.0f : p_continue;
 }
 
-__global__ void __launch_bounds__(kShadeThreads, 1) k_shade(PathBatch pb, const WaveTables wt, uint32_t bounce) {
+__global__ void __launch_bounds__(kShadeThreads, kShadeBlocksPerSM) k_shade(PathBatch pb, const WaveTables wt, uint32_t bounce) {
   __shared__ Segment segs[nb::kMaxWaveSegments];
   __shared__ uint32_t append_sh[2 * kDirBins];
   stage_segments(segs, wt);
