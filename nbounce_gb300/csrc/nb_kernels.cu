@@ -529,51 +529,55 @@ __device__ __forceinline__ void tile_pixel(uint32_t i, uint32_t W, uint32_t H, u
 // frame is one wave, so all samples are present): 12-14% faster traversal.
 constexpr uint32_t kSampleGroup = 64;
 
-// One camera ray per path.  Path ids stay row-major per sample (pixel = id % (W*H)); the
-// queue lists them by sample group and tile order (tile_pixel), which every later kernel
-// follows through the path id each ray carries.
+// Camera ray of queue entry q (pathtracing.wgsl:245-255): origin with the path id in .w,
+// direction with the scene index in .w.  Path ids stay row-major per sample (pixel = id %
+// (W*H)); the queue lists them by sample group and tile order (tile_pixel), which every later
+// kernel follows through the path id each ray carries.  segs: the wave's segments.
+__device__ __forceinline__ void camera_ray(const Segment* segs, const WaveTables& wt, const PathBatch& pb, uint32_t q,
+                                           float4& o4, float4& d4) {
+  const Segment sg = segs[find_segment<false>(segs, wt.n_segs, q)];
+  const JobParams& jp = wt.jobs[sg.job];
+  const uint32_t local = q - sg.path_begin;
+  // the segment's samples in groups of kSampleGroup: the queue runs over one group's samples
+  // of a pixel, then the next pixel in tile order (a last, smaller group the same way)
+  const uint32_t span = kSampleGroup * jp.npix, full = sg.n_samples / kSampleGroup;
+  uint32_t plane, order;
+  if (local < full * span) {
+    const uint32_t grp = local / span, j = local - grp * span;
+    plane = grp * kSampleGroup + j % kSampleGroup;
+    order = j / kSampleGroup;
+  } else {
+    const uint32_t g = sg.n_samples - full * kSampleGroup, j = local - full * span;
+    plane = full * kSampleGroup + j % g;
+    order = j / g;
+  }
+  uint32_t x, y;
+  tile_pixel(order, jp.width, jp.height, &x, &y);
+  const uint32_t p = sg.path_begin + plane * jp.npix + y * jp.width + x;
+  const uint32_t sample = sg.first_sample + plane;
+  const float4 shift = hash4f(x, y);
+  const float4 sb = sobol_read(pb.sobol, pb.sobol_entries, sample * kLdsStride);
+  const float jx = fract(sb.x + shift.x), jy = fract(sb.y + shift.y);
+  V3 o, d;
+  generate_ray(x, y, jp.width, jp.height, jx, jy, jp.c2w, &o, &d);
+  o4 = make_float4(o.x, o.y, o.z, __uint_as_float(p));
+  d4 = make_float4(d.x, d.y, d.z, __uint_as_float(jp.scene));
+}
+
+// Start of a wave: the bounce counters and work cursors, and (kWaveZeroRadiance: waves whose
+// shading adds to radiance) every path's radiance zeroed.  The camera rays themselves are made
+// by the bounce-0 traversal, which writes them to the queue for shading (camera_ray).  A
+// segment's queue positions and path ids cover the same range, so zeroing by queue position
+// clears every path's radiance with coalesced stores.
 __global__ void __launch_bounds__(256) k_raygen(PathBatch pb, const WaveTables wt) {
-  __shared__ Segment segs[nb::kMaxWaveSegments];
-  stage_segments(segs, wt);
   const uint32_t n = wt.n_paths;
   if (blockIdx.x == 0 && threadIdx.x < kMaxBounceSlots) {
     pb.counts[threadIdx.x] = threadIdx.x == 0 ? n : 0u;
     pb.fetch[threadIdx.x] = 0u;
   }
-  for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x) {
-    const Segment sg = segs[find_segment<false>(segs, wt.n_segs, q)];
-    const JobParams& jp = wt.jobs[sg.job];
-    const uint32_t local = q - sg.path_begin;
-    // the segment's samples in groups of kSampleGroup: the queue runs over one group's samples
-    // of a pixel, then the next pixel in tile order (a last, smaller group the same way)
-    const uint32_t span = kSampleGroup * jp.npix, full = sg.n_samples / kSampleGroup;
-    uint32_t plane, order;
-    if (local < full * span) {
-      const uint32_t grp = local / span, j = local - grp * span;
-      plane = grp * kSampleGroup + j % kSampleGroup;
-      order = j / kSampleGroup;
-    } else {
-      const uint32_t g = sg.n_samples - full * kSampleGroup, j = local - full * span;
-      plane = full * kSampleGroup + j % g;
-      order = j / g;
-    }
-    uint32_t x, y;
-    tile_pixel(order, jp.width, jp.height, &x, &y);
-    const uint32_t p = sg.path_begin + plane * jp.npix + y * jp.width + x;
-    const uint32_t sample = sg.first_sample + plane;
-    const float4 shift = hash4f(x, y);
-    const float4 sb = sobol_read(pb.sobol, pb.sobol_entries, sample * kLdsStride);
-    const float jx = fract(sb.x + shift.x), jy = fract(sb.y + shift.y);
-    V3 o, d;
-    generate_ray(x, y, jp.width, jp.height, jx, jy, jp.c2w, &o, &d);
-    pb.q_o[0][q] = make_float4(o.x, o.y, o.z, __uint_as_float(p));
-    pb.q_d[0][q] = make_float4(d.x, d.y, d.z, __uint_as_float(jp.scene));
-    // the camera ray's throughput is (1, 1, 1) with lobe density 0 (q_t.w): the shade kernels
-    // take it as such at bounce 0 instead of reading it from the queue.  A segment's queue
-    // positions and path ids cover the same range, so zeroing by queue position clears every
-    // path's radiance with coalesced stores (by path id, the lanes of a warp would store 16
-    // bytes each, npix apart)
-    if (wt.flags & nb::kWaveZeroRadiance) pb.radiance[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
+  if (wt.flags & nb::kWaveZeroRadiance) {
+    for (uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x)
+      pb.radiance[q] = make_float4(0.0f, 0.0f, 0.0f, 0.0f);
   }
 }
 
@@ -612,7 +616,9 @@ __global__ void __launch_bounds__(kTraceThreads, kRefill ? 8 : 7) k_trace_wave(P
   const int lane = threadIdx.x & 31;
   uint32_t st = 0;
   TraceCount cnt;
-  if (!kRefill) {
+  if (!kRefill) {  // bounce 0: camera rays, made here and written to the queue for shading
+    __shared__ Segment segs[nb::kMaxWaveSegments];
+    stage_segments(segs, wt);
     while (true) {
       uint32_t base = 0;
       if (lane == 0) base = atomicAdd(pb.fetch + bounce, 32u);
@@ -620,7 +626,10 @@ __global__ void __launch_bounds__(kTraceThreads, kRefill ? 8 : 7) k_trace_wave(P
       if (base >= n) break;
       const uint32_t i = base + lane;
       if (i < n) {
-        const float4 o = qo[i], d = qd[i];
+        float4 o, d;
+        camera_ray(segs, wt, pb, i, o, d);
+        pb.q_o[0][i] = o;
+        pb.q_d[0][i] = d;
         Hit h;
         st |= trace_ray<false, kCount>(kSingle ? wt.scenes[0] : scenes[__float_as_uint(d.w)], xyz(o), xyz(d), h,
                                        &cnt);
@@ -1578,7 +1587,7 @@ cudaError_t launch_trace_rays(const nbd::DevScene& s, const float* rays, uint32_
 }
 
 cudaError_t launch_raygen(const PathBatch& pb, const WaveTables& wt, int sms, cudaStream_t st) {
-  int g = (int)std::min<uint64_t>((wt.n_paths + 255) / 256, (uint64_t)sms * 16);
+  int g = (wt.flags & kWaveZeroRadiance) ? (int)std::min<uint64_t>((wt.n_paths + 255) / 256, (uint64_t)sms * 16) : 1;
   nbd::k_raygen<<<g < 1 ? 1 : g, 256, 0, st>>>(pb, wt);
   return cudaGetLastError();
 }
