@@ -271,32 +271,13 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
   key[j] = max(key[i], key[j]);                    \
   key[i] = lo_;                                    \
 }
-  if (n_push > 1) {
-    NB_CX(0, 2) NB_CX(1, 3) NB_CX(4, 6) NB_CX(5, 7)
-    NB_CX(0, 4) NB_CX(1, 5) NB_CX(2, 6) NB_CX(3, 7)
-    NB_CX(0, 1) NB_CX(2, 3) NB_CX(4, 5) NB_CX(6, 7)
-    NB_CX(2, 4) NB_CX(3, 5)
-    NB_CX(1, 4) NB_CX(3, 6)
-    NB_CX(1, 2) NB_CX(3, 4) NB_CX(5, 6)
-  } else if (n_push == 1) {  // move the single key to the front
-    uint32_t m = key[0];
-#pragma unroll
-    for (int k = 1; k < 8; ++k) m = min(m, key[k]);
-#pragma unroll
-    for (int k = 1; k < 8; ++k) key[k] = 0xFFFFFFFFu;
-    key[0] = m;
-  }
-#undef NB_CX
   // push far to near; the nearest inner child is visited next without a push
-#pragma unroll
-  for (int k = 7; k >= 0; --k) {
-    const uint32_t kk = key[k];
-    if (kk == 0xFFFFFFFFu) continue;
+  auto take = [&](uint32_t kk, bool nearest) {
     const float d = __uint_as_float(kk & ~7u);
     const uint32_t slot = kk & 7u;
     const uint32_t meta = ((slot < 4 ? m0 : m1) >> (8 * (slot & 3))) & 0xFFu;
     const uint32_t ref = (meta & 0x80u) ? child_base + (meta & 7u) : (kInstanceBit | (prim_base + (meta & 31u)));
-    if (k == 0 && (meta & 0x80u)) {
+    if (nearest && (meta & 0x80u)) {
       node = ref;
       have_node = true;
       next_d = d;
@@ -307,7 +288,25 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
     } else {
       status |= kStatusStackOverflow;
     }
+  };
+  if (n_push == 1) {  // the single hit child: no sort, no loop over the empty keys
+    uint32_t m = key[0];
+#pragma unroll
+    for (int k = 1; k < 8; ++k) m = min(m, key[k]);
+    take(m, true);
+  } else if (n_push > 1) {
+    NB_CX(0, 2) NB_CX(1, 3) NB_CX(4, 6) NB_CX(5, 7)
+    NB_CX(0, 4) NB_CX(1, 5) NB_CX(2, 6) NB_CX(3, 7)
+    NB_CX(0, 1) NB_CX(2, 3) NB_CX(4, 5) NB_CX(6, 7)
+    NB_CX(2, 4) NB_CX(3, 5)
+    NB_CX(1, 4) NB_CX(3, 6)
+    NB_CX(1, 2) NB_CX(3, 4) NB_CX(5, 6)
+#pragma unroll
+    for (int k = 7; k >= 0; --k) {
+      if (key[k] != 0xFFFFFFFFu) take(key[k], k == 0);
+    }
   }
+#undef NB_CX
   // ---- BLAS leaves: Moller-Trumbore (raytracing_sw.wgsl:51-78, 274-286) ----
   while (leaf_mask) {
     const int k = __ffs(leaf_mask) - 1;
