@@ -51,11 +51,17 @@ constexpr uint32_t kInstanceBit = 0x80000000u;
 __device__ __forceinline__ float4 ld4(const float4* p) { return __ldg(p); }
 __device__ __forceinline__ uint32_t f2u(float x) { return __float_as_uint(x); }
 
-// direction reciprocal for box tests: components below 1e-20 in magnitude are nudged to
-// +-1e-20 so that every plane distance stays finite (triangle tests use the true direction)
+// Direction reciprocal for box tests only: components below 1e-20 in magnitude are nudged to
+// +-1e-20 so that every plane distance stays finite (triangle tests use the true direction).
+// The hardware's approximate reciprocal (relative error <= 2^-23, no slow path) instead of a
+// correctly rounded division: the box test's per-axis margins cover the extra rounding (see
+// trace_step), and the correctly rounded division cost 2.2 ms of the benchmark frame's traversal.
 __device__ __forceinline__ float safe_rcp(float d) {
   const float m = 1e-20f;
-  return 1.0f / (fabsf(d) < m ? copysignf(m, d) : d);
+  const float x = fabsf(d) < m ? copysignf(m, d) : d;
+  float r;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+  return r;
 }
 
 struct Hit {
@@ -103,18 +109,43 @@ __device__ __forceinline__ void trace_begin(TraceState& t, uint2* stack, const D
   t.iter = 0;
 }
 
-// Where trace_step reads the world ray when it enters or leaves an instance: the traversal
-// state's registers (WorldRegs), or a per-warp array in shared memory (WorldShared,
-// component-major so that the 32 lanes' loads hit distinct banks), which keeps six registers
-// free in the kernels whose register budget is tightest.
+// Where trace_step reads the world ray and its box-test reciprocal when it enters or leaves an
+// instance.  A per-warp array in shared memory, component-major so that the 32 lanes' loads hit
+// distinct banks, kWorldFloats floats: origin, direction, reciprocal direction x 32 lanes.
+//   WorldShared  all three in shared memory: keeps six registers free in the lane-refill
+//                kernels, whose register budget is tightest;
+//   WorldMixed   origin and direction in registers, the reciprocal in shared memory (the
+//                camera-ray kernel, which enters and leaves instances at most steps);
+//   WorldRegs    origin and direction in registers, the reciprocal recomputed (caller rays
+//                without refill).
+// Keeping the reciprocal instead of recomputing it when a BLAS is left measured 2.3 ms faster
+// traversal on the benchmark frame.
+constexpr int kWorldFloats = 9 * 32;
+constexpr int kTraceWarps = 4;  // every traversal kernel runs blocks of 128 threads
+constexpr int kTraceThreads = 32 * kTraceWarps;
 struct WorldRegs {
   const TraceState& t;
   __device__ __forceinline__ V3 o() const { return t.wo; }
   __device__ __forceinline__ V3 d() const { return t.wd; }
+  __device__ __forceinline__ V3 inv() const { return V3{safe_rcp(t.wd.x), safe_rcp(t.wd.y), safe_rcp(t.wd.z)}; }
 };
-constexpr int kWorldFloats = 6 * 32;  // one warp's world rays: ox, oy, oz, dx, dy, dz x 32 lanes
-constexpr int kTraceWarps = 4;  // every traversal kernel runs blocks of 128 threads
-constexpr int kTraceThreads = 32 * kTraceWarps;
+// a warp's reciprocal directions: kInvFloats floats, component-major
+constexpr int kInvFloats = 3 * 32;
+__device__ __forceinline__ V3 world_inv(const float* w) {
+  const uint32_t l = threadIdx.x & 31u;
+  return V3{w[l], w[32 + l], w[64 + l]};
+}
+__device__ __forceinline__ void set_world_inv(float* w, V3 r) {
+  const uint32_t l = threadIdx.x & 31u;
+  w[l] = r.x; w[32 + l] = r.y; w[64 + l] = r.z;
+}
+struct WorldMixed {
+  const TraceState& t;
+  const float* w;  // kInvFloats
+  __device__ __forceinline__ V3 o() const { return t.wo; }
+  __device__ __forceinline__ V3 d() const { return t.wd; }
+  __device__ __forceinline__ V3 inv() const { return world_inv(w); }
+};
 struct WorldShared {
   float* w;
   __device__ __forceinline__ V3 o() const {
@@ -125,11 +156,13 @@ struct WorldShared {
     const uint32_t l = threadIdx.x & 31u;
     return V3{w[96 + l], w[128 + l], w[160 + l]};
   }
+  __device__ __forceinline__ V3 inv() const { return world_inv(w + 192); }
   __device__ __forceinline__ void set(V3 o, V3 d) const {
     const uint32_t l = threadIdx.x & 31u;
     w[l] = o.x; w[32 + l] = o.y; w[64 + l] = o.z;
     w[96 + l] = d.x; w[128 + l] = d.y; w[160 + l] = d.z;
   }
+  __device__ __forceinline__ void set_inv(V3 r) const { set_world_inv(w + 192, r); }
 };
 
 // Work counters of the instrumented traversal (kCount instantiations only): what the device
@@ -162,7 +195,7 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
         in_blas = false;
         const V3 wd = wr.d();
         ro = wr.o(); rd = wd;
-        rinv = V3{safe_rcp(wd.x), safe_rcp(wd.y), safe_rcp(wd.z)};
+        rinv = wr.inv();
       }
       if (sp == 0) {
         done = true;
@@ -209,14 +242,15 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
   // and its distance taken as fma(F, a, b - 2^15 a), one rounding more than fma(q, a, b): the
   // folded constant differs from b - 2^15 a by at most 2^-24 (|b| + 2^15 |a|), so each plane's
   // distance lies within e = 2^-24 (3 |b| + (2^15 + 510) |a|) of fma(q, a, b).  Near-plane
-  // constants are lowered and far-plane constants raised by d = |a| / 128 + |b| / 2^20 per
-  // axis.  d - e >= 7.7e-7 |b| + 0.0058 |a| >= 4e-7 (|b| + 255 |a|) >= 4e-7 |t| for every plane
-  // t = b + q a of the node: besides the fold, the margin covers the rounding of the plane
-  // evaluation against the exact reference box (a relative 4e-7 of the distance), so that a
-  // box never rejects a ray the reference box accepts.
-  const float dx = fmaf(fabsf(ax), 0.0078125f, fabsf(bx) * 9.5367431640625e-7f);
-  const float dy = fmaf(fabsf(ay), 0.0078125f, fabsf(by) * 9.5367431640625e-7f);
-  const float dz = fmaf(fabsf(az), 0.0078125f, fabsf(bz) * 9.5367431640625e-7f);
+  // constants are lowered and far-plane constants raised by d = |a| / 128 + |b| / 2^19 per
+  // axis.  For every plane t = b + q a of the node (|t| <= |b| + 255 |a|) the margin covers
+  // the fold (e <= 1.8e-7 |b| + 0.002 |a|), the approximate reciprocal (<= 2^-22 |t|) and the
+  // rounding of the plane evaluation against the exact reference box (4e-7 |t|): together
+  // at most 8.2e-7 |b| + 0.0022 |a| <= d, so a box never rejects a ray the reference box
+  // accepts.
+  const float dx = fmaf(fabsf(ax), 0.0078125f, fabsf(bx) * 1.9073486328125e-6f);
+  const float dy = fmaf(fabsf(ay), 0.0078125f, fabsf(by) * 1.9073486328125e-6f);
+  const float dz = fmaf(fabsf(az), 0.0078125f, fabsf(bz) * 1.9073486328125e-6f);
   const float cx = fmaf(-32768.0f, ax, bx), cy = fmaf(-32768.0f, ay, by), cz = fmaf(-32768.0f, az, bz);
   const float cnx = cx - dx, cfx = cx + dx, cny = cy - dy, cfy = cy + dy, cnz = cz - dz, cfz = cz + dz;
   const uint32_t child_base = f2u(q1.x), prim_base = f2u(q1.y);
@@ -398,6 +432,7 @@ __device__ __forceinline__ uint32_t trace_refill(uint32_t* fetch, uint32_t n, Lo
           load(r, o, d, sidx);
           trace_begin(t, stack, scene(sidx), o, d);
           wr.set(o, d);
+          wr.set_inv(t.rinv);
         }
       }
     }
@@ -617,6 +652,7 @@ __global__ void __launch_bounds__(kTraceThreads, kRefill ? 8 : 7) k_trace_wave(P
   TraceCount cnt;
   if (!kRefill) {  // bounce 0: camera rays, made here and written to the queue for shading
     __shared__ Segment segs[nb::kMaxWaveSegments];
+    __shared__ float inv_c[kTraceWarps][kInvFloats];
     stage_segments(segs, wt);
     while (true) {
       uint32_t base = 0;
@@ -629,11 +665,18 @@ __global__ void __launch_bounds__(kTraceThreads, kRefill ? 8 : 7) k_trace_wave(P
         camera_ray(segs, wt, pb, i, o, d);
         pb.q_o[0][i] = o;
         pb.q_d[0][i] = d;
-        Hit h;
-        st |= trace_ray<false, kCount>(kSingle ? wt.scenes[0] : scenes[__float_as_uint(d.w)], xyz(o), xyz(d), h,
-                                       &cnt);
-        pb.hits[i] = make_float4(h.t, h.u, h.v, __uint_as_float(h.tri));
-        pb.hit_inst[i] = h.inst;
+        const DevScene& sc0 = kSingle ? wt.scenes[0] : scenes[__float_as_uint(d.w)];
+        TraceState t;
+        uint2 stack[kStackSize + 2];
+        trace_begin(t, stack, sc0, xyz(o), xyz(d));
+        set_world_inv(inv_c[threadIdx.x >> 5], t.rinv);
+        const WorldMixed wm{t, inv_c[threadIdx.x >> 5]};
+        while (trace_step<false, kCount>(t, stack, sc0, &cnt, wm)) {
+        }
+        st |= t.status;
+        const uint2 uv = stack[kHitSlot], ti = stack[kHitSlot + 1];
+        pb.hits[i] = make_float4(t.t_hit, __uint_as_float(uv.x), __uint_as_float(uv.y), __uint_as_float(ti.x));
+        pb.hit_inst[i] = ti.y;
       }
     }
   } else {
