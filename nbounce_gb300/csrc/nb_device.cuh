@@ -30,6 +30,21 @@ constexpr uint32_t kLdsPerBounce = 2u;
 constexpr uint32_t kStatusStackOverflow = 1u << 0;
 constexpr uint32_t kStatusIterationCap = 1u << 1;
 
+// Correctly rounded 1 / b for b in [kRcpNewtonMin, kRcpNewtonMax) without a division: the
+// hardware's approximate reciprocal refined by one Newton-Raphson step in fused multiply-adds,
+// e = 1 - b y, y + y e (Markstein, "Computation of elementary functions on the IBM RISC
+// System/6000 processor", IBM J. Res. Dev. 34(1), 1990).  Compared bit for bit with the
+// correctly rounded division for every float of that range by tests/test_gpu_reciprocal.py
+// (1,280,586,633 values, no difference); outside it the caller divides.  Below 2^126 the
+// reciprocal stays a normal number, which the flush-to-zero approximation needs.
+constexpr float kRcpNewtonMin = 1e-8f;  // kEps: the smallest determinant a triangle test divides by
+constexpr float kRcpNewtonMax = 0x1p126f;
+__device__ __forceinline__ float rcp_newton(float b) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(b));
+  return fmaf(fmaf(-b, y, 1.0f), y, y);
+}
+
 struct V3 {
   float x, y, z;
 };

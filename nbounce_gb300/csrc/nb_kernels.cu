@@ -355,7 +355,8 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
       const V3 hv = cross(rd, e2);
       const float det = dot(e1, hv);
       if (det < kEps) continue;
-      const float inv_det = 1.0f / det;
+      // det >= kEps here; 1 / det correctly rounded, as the reference arithmetic divides
+      const float inv_det = det < kRcpNewtonMax ? rcp_newton(det) : 1.0f / det;
       const V3 sv = ro - xyz(a);
       const float u = inv_det * dot(sv, hv);
       if (u < 0.0f || u > 1.0f) continue;
