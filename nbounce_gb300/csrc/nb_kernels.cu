@@ -406,7 +406,7 @@ __device__ __forceinline__ uint32_t trace_ray(const DevScene& s, const V3 wo, co
 // (secondary and shadow rays, caller rays): their traversal lengths differ widely, and without
 // refill most lanes would idle while the longest ray of each 32 finishes.  Refill changes only
 // which lane traces a ray, not its result.
-constexpr uint32_t kRefillIdle = 8;
+constexpr uint32_t kRefillIdle = 6;
 template <bool kAny, bool kCount, class Load, class SceneOf, class Finish>
 __device__ __forceinline__ uint32_t trace_refill(uint32_t* fetch, uint32_t n, Load load, SceneOf scene, Finish finish,
                                                  TraceCount* cnt, float* world) {
