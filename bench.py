@@ -50,11 +50,11 @@ if ROOT not in sys.path:
 METRIC = "Mrays/s (primary + extension rays), 1920x1080 64spp 8 bounces"
 # DRAM bytes (read + write) per traversal query of k_trace_wave over all bounces of a frame,
 # from one ncu capture of the same scene at 480x270, 64 spp (nine launches, 12,435,256 rays,
-# 980.6 MB read + 479.0 MB written); the roofline scales it to a launch by the launch's rays
-TRACE_DRAM_BYTES_PER_RAY = 117.4
+# 982.7 MB read + 480.3 MB written); the roofline scales it to a launch by the launch's rays
+TRACE_DRAM_BYTES_PER_RAY = 117.7
 # issue utilisation of the same capture (smsp__issue_active.avg.pct_of_peak_sustained_active):
 # camera rays (k_trace_wave<1,0,0>) and bounce 1 (the lane-refill kernel)
-TRACE_ISSUE_ACTIVE_PCT = {"camera_rays": 77.3, "bounce_1": 72.4}
+TRACE_ISSUE_ACTIVE_PCT = {"camera_rays": 77.4, "bounce_1": 71.8}
 UNIT = "Mrays/s"
 WORKLOAD = "instanced 16 meshes / 1024 instances, 1920x1080, 64 spp, 8 bounces, equirect sky"
 # bytes the device layout fetches per unit of traversal work (nb_trace_counters): an 8-wide
