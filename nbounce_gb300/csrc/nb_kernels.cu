@@ -174,7 +174,8 @@ struct TraceCount {
 
 // One traversal step: pop the next entry when no node is pending, then test one 8-wide node
 // and its leaf triangles.  Returns false once the ray is finished (stack empty, an any-hit
-// found, or the iteration cap reached).  wr gives the world ray (WorldRegs / WorldShared).
+// found, or the iteration cap reached).  wr gives the world ray (WorldRegs, WorldMixed or
+// WorldShared).
 template <bool kAny, bool kCount, class World>
 __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const DevScene& s, TraceCount* cnt,
                                            const World& wr) {
@@ -456,9 +457,9 @@ __device__ __forceinline__ uint32_t trace_refill(uint32_t* fetch, uint32_t n, Lo
 // instantiations fit 64 registers without spills and run 8 blocks per SM, closest hit without
 // refill 7 blocks at 72 registers.
 template <bool kAny, bool kRefill>
-__global__ void __launch_bounds__(kTraceThreads, kRefill || kAny ? 8 : 7) k_trace_rays(DevScene s, const float4* __restrict__ rays, uint32_t n,
-                                                     float4* __restrict__ hits, uint32_t* __restrict__ inst,
-                                                     uint32_t* __restrict__ fetch, uint32_t* __restrict__ status) {
+__global__ void __launch_bounds__(kTraceThreads, kRefill || kAny ? 8 : 7)
+    k_trace_rays(DevScene s, const float4* __restrict__ rays, uint32_t n, float4* __restrict__ hits,
+                 uint32_t* __restrict__ inst, uint32_t* __restrict__ fetch, uint32_t* __restrict__ status) {
   const int lane = threadIdx.x & 31;
   uint32_t st = 0;
   if (kRefill) {
