@@ -256,7 +256,9 @@ int nb_pathtracer_last_stats(const nb_pathtracer* pt, uint64_t* rays, uint32_t* 
 
 /* Per-kernel CUDA-event timing of the pass's launches, recorded on the launch stream (the
  * reference leaves GPU timestamps off, pathtracer.rs:229; "timer queries" is an open item of
- * its feature list).  Off by default. */
+ * its feature list).  Off by default.  raygen_ms covers the wave's start (counters, and radiance
+ * zeroed for NEE and cache waves); camera rays are made inside the bounce-0 traversal and count
+ * in trace_ms. */
 typedef struct nb_kernel_times {
   double raygen_ms, trace_ms, shade_ms, accumulate_ms;
   uint64_t raygen_launches, trace_launches, shade_launches, accumulate_launches;
