@@ -618,24 +618,25 @@ __global__ void __launch_bounds__(256) k_raygen(PathBatch pb, const WaveTables w
 }
 
 // kSingle: every ray of the wave uses wt.scenes[0]; else the scene index carried in q_d.w.
-// Persistent warps take 32 consecutive rays per atomic and trace them together: consecutive
-// queue entries are 32 samples of one pixel (camera rays) or come from
-// one small patch of the image with one direction bin (later bounces), so the lanes of a warp
-// walk largely the same nodes (shared cache lines, agreeing branches).  Refilling finished lanes one by one with
-// unrelated rays, with or without a warp-wide sync per node step, measured 11-30% slower.
+// Bounce 0 (camera rays): persistent warps take 32 consecutive queue entries per atomic - 32
+// samples of one pixel - make each lane's camera ray (camera_ray), write it to the queue for
+// shading and trace the 32 together, so the lanes walk largely the same nodes (shared cache
+// lines, agreeing branches).  The world ray stays in registers, its box-test reciprocal in
+// shared memory (WorldMixed).
 // kCount: the instrumented variant, which also adds the TraceCount totals of the launch to
 // counters[8 * bounce + 0..4] (run only when a caller asks for the counters).
 //
 // kRefill (bounces >= 1): a lane whose ray finished does not wait for the rest of its warp's
 // 32 rays; once kRefillIdle lanes of the warp are idle, the warp takes that many new rays with
-// one atomic and those lanes start on them.  Secondary rays of a warp come from different
-// pixels and surfaces and their traversal lengths differ widely, so without refill most lanes
-// idle while the longest ray finishes (11 of 32 lanes active per instruction on bounce 1).
-// Camera rays keep whole-warp chunks: a warp's 32 samples of one pixel finish together, and
-// refilling them measured 9% slower traversal.  Refill changes only which lane traces a ray,
-// not its result.  The refill instantiation fits 64 registers without spills, so it runs 8
-// blocks of 128 per SM instead of 7 at 72 (measured: secondary-ray traversal 2.6 ms faster per
-// frame; 6 blocks at 80 registers 5.2 ms slower, 9 blocks at 56 spills).
+// one atomic and those lanes start on them (trace_refill, world rays in shared memory).
+// Secondary rays of a warp come from different pixels and surfaces and their traversal lengths
+// differ widely, so without refill most lanes idle while the longest ray finishes (11 of 32
+// lanes active per instruction on bounce 1).  Camera rays keep whole-warp chunks: a warp's 32
+// samples of one pixel finish together, and refilling them measured 9% slower traversal.
+// Refill changes only which lane traces a ray, not its result.  The refill instantiation fits
+// 64 registers without spills, so it runs 8 blocks of 128 per SM instead of 7 at 72 (measured:
+// secondary-ray traversal 2.6 ms faster per frame; 6 blocks at 80 registers 5.2 ms slower, 9
+// blocks at 56 spills).
 template <bool kSingle, bool kCount, bool kRefill>
 __global__ void __launch_bounds__(kTraceThreads, kRefill ? 8 : 7) k_trace_wave(PathBatch pb, const WaveTables wt,
                                                                      uint32_t bounce,
