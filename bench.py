@@ -644,6 +644,17 @@ def trace_roofline(pt, scene, cam, env, desc, kt, steps, rays_per_step, sh, of):
         return {**{k: round(sum(x[k] for x in xs) / r, 3) for k in keys},
                 "bytes": round(sum(bytes_of(x) for x in xs) / r, 1), "rays": int(r)}
 
+    def lanes(xs):
+        # how a warp's 32 lanes share the node steps (the instrumented kernel's warp-step counts)
+        tot = {k: sum(x[k] for x in xs) for k in ("warp_steps", "lane_steps", "leaf_steps", "leaf_lanes",
+                                                   "leaf_warp_triangles", "triangle_tests")}
+        ws, ls = max(1, tot["warp_steps"]), max(1, tot["leaf_steps"])
+        return {"lanes_per_step": round(tot["lane_steps"] / ws, 2),
+                "leaf_step_frac": round(tot["leaf_steps"] / ws, 3),
+                "leaf_lanes_per_leaf_step": round(tot["leaf_lanes"] / ls, 2),
+                "warp_triangle_iterations_per_leaf_step": round(tot["leaf_warp_triangles"] / ls, 2),
+                "leaf_loop_lane_use": round(tot["triangle_tests"] / max(1, 32 * tot["leaf_warp_triangles"]), 3)}
+
     counted_rays = sum(x["rays"] for x in c)
     total_bytes = sum(bytes_of(x) for x in c)
     launches = max(1, kt["trace_launches"]) / steps
@@ -658,6 +669,7 @@ def trace_roofline(pt, scene, cam, env, desc, kt, steps, rays_per_step, sh, of):
             "bytes_per_launch": round(bytes_per_launch), "avg_launch_ms": round(avg_launch_ms, 4),
             "counted_rays_per_step": int(counted_rays),
             "device_work_per_ray": {"bounce_0": per_ray(c[:1]), "bounces_1_plus": per_ray(c[1:])},
+            "warp_lanes": {"bounce_0": lanes(c[:1]), "bounces_1_plus": lanes(c[1:])},
             "rays_per_bounce": [x["rays"] for x in c],
             "traffic_note": "ncu dram bytes per ray of all trace launches of the 480x270 64-spp small case "
                             "(profiles/k_trace_wave__instanced_480x270_64spp.md) x rays per launch",

@@ -284,6 +284,11 @@ typedef struct nb_trace_counters {
   uint64_t triangle_tests;       /* Moller-Trumbore tests */
   uint64_t instance_entries;     /* world-to-local ray transforms */
   uint64_t stack_pushes;         /* traversal stack entries written */
+  /* how the 32 lanes of a warp share the node steps (lanes that test a node together count
+   * one warp step): lane_steps / warp_steps = lanes per step; leaf_steps = warp steps in which
+   * some lane tests leaf triangles, leaf_lanes = the lanes that do, leaf_warp_triangles = the
+   * sum over those steps of the largest triangle count of a lane (the warp's iterations) */
+  uint64_t warp_steps, lane_steps, leaf_steps, leaf_lanes, leaf_warp_triangles;
 } nb_trace_counters;
 int nb_pathtracer_enable_trace_counters(nb_pathtracer* pt, int enable);
 /* Copies the counters of bounces 0 .. n_bounces-1 since the last reset into out[0 .. n_bounces-1]

@@ -74,7 +74,9 @@ class NbKernelTimes(C.Structure):
 
 class NbTraceCounters(C.Structure):
     _fields_ = [("rays", C.c_uint64), ("tlas_node_tests", C.c_uint64), ("blas_node_tests", C.c_uint64),
-                ("triangle_tests", C.c_uint64), ("instance_entries", C.c_uint64), ("stack_pushes", C.c_uint64)]
+                ("triangle_tests", C.c_uint64), ("instance_entries", C.c_uint64), ("stack_pushes", C.c_uint64),
+                ("warp_steps", C.c_uint64), ("lane_steps", C.c_uint64), ("leaf_steps", C.c_uint64),
+                ("leaf_lanes", C.c_uint64), ("leaf_warp_triangles", C.c_uint64)]
 
 
 NB_CACHE_PARAMS = 21504

@@ -767,7 +767,7 @@ int nb_pathtracer_enable_trace_counters(nb_pathtracer* pt, int enable) {
   }
   if (pt->d_trace_counts) return NB_OK;
   void* p = nullptr;
-  const size_t bytes = 8 * kMaxBounceSlots * sizeof(unsigned long long);
+  const size_t bytes = nb::kTraceCounterSlots * kMaxBounceSlots * sizeof(unsigned long long);
   int rc = pt->counter_mem.alloc(bytes, &p);
   if (rc) return rc;
   NB_CUDA(cudaMemset(p, 0, bytes), "cudaMemset(trace counters)");
@@ -781,13 +781,13 @@ int nb_pathtracer_trace_counters(nb_pathtracer* pt, nb_trace_counters* out, uint
   if (!pt->d_trace_counts) return fail(NB_ERR_INVALID_ARG, "trace counters are not enabled");
   if (n_bounces > kMaxBounceSlots) return fail(NB_ERR_INVALID_ARG, "at most %u bounce slots", kMaxBounceSlots);
   cudaStream_t st = (cudaStream_t)stream;
-  std::vector<unsigned long long> h(8 * kMaxBounceSlots);
+  std::vector<unsigned long long> h(nb::kTraceCounterSlots * kMaxBounceSlots);
   NB_CUDA(cudaMemcpyAsync(h.data(), pt->d_trace_counts, h.size() * sizeof(h[0]), cudaMemcpyDeviceToHost, st),
           "cudaMemcpyAsync(trace counters)");
   NB_CUDA(cudaStreamSynchronize(st), "cudaStreamSynchronize");
   for (uint32_t b = 0; b < n_bounces; ++b) {
-    const unsigned long long* c = h.data() + 8 * b;
-    out[b] = nb_trace_counters{c[5], c[0], c[1], c[2], c[3], c[4]};
+    const unsigned long long* c = h.data() + nb::kTraceCounterSlots * b;
+    out[b] = nb_trace_counters{c[5], c[0], c[1], c[2], c[3], c[4], c[6], c[7], c[8], c[9], c[10]};
   }
   if (reset) NB_CUDA(cudaMemsetAsync(pt->d_trace_counts, 0, h.size() * sizeof(h[0]), st), "cudaMemsetAsync");
   return NB_OK;

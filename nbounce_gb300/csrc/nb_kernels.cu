@@ -167,10 +167,18 @@ struct WorldShared {
 
 // Work counters of the instrumented traversal (kCount instantiations only): what the device
 // layout fetches per ray - 80-byte wide nodes of the TLAS and the BLASes, 48-byte triangle
-// records, 64-byte instance records - and the 8-byte stack entries pushed (each later popped).
+// records, 64-byte instance records - and the 8-byte stack entries pushed (each later popped);
+// and how the lanes of a warp share the node steps: warp steps (lanes that test a node
+// together count one step, recorded by the lowest of them) with their lanes, and of those the
+// steps in which some lane tests leaf triangles, with the lanes that do and the largest
+// triangle count among them (the warp's iterations of the leaf loop).
 struct TraceCount {
   uint32_t tlas_nodes = 0, blas_nodes = 0, tris = 0, insts = 0, pushes = 0;
+  uint32_t warp_steps = 0, lane_steps = 0, leaf_steps = 0, leaf_lanes = 0, leaf_trips = 0;
 };
+__device__ __forceinline__ bool lowest_active(uint32_t mask) {
+  return (threadIdx.x & 31u) == (uint32_t)(__ffs(mask) - 1);
+}
 
 // One traversal step: pop the next entry when no node is pending, then test one 8-wide node
 // and its leaf triangles.  Returns false once the ray is finished (stack empty, an any-hit
@@ -231,7 +239,14 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
   have_node = false;
 
   // ---- one 8-wide node: quantised slab tests of all children ----
-  if (kCount) ++(in_blas ? cnt->blas_nodes : cnt->tlas_nodes);
+  if (kCount) {
+    ++(in_blas ? cnt->blas_nodes : cnt->tlas_nodes);
+    const uint32_t together = __activemask();
+    if (lowest_active(together)) {
+      ++cnt->warp_steps;
+      cnt->lane_steps += (uint32_t)__popc(together);
+    }
+  }
   const float4* np = (in_blas ? s.blas_wide : s.tlas_wide) + 5 * (size_t)node;
   const float4 q0 = ld4(np), q1 = ld4(np + 1), q2 = ld4(np + 2), q3 = ld4(np + 3), q4 = ld4(np + 4);
   const uint32_t eb = f2u(q0.w);
@@ -342,6 +357,21 @@ __device__ __forceinline__ bool trace_step(TraceState& t, uint2* stack, const De
     }
   }
 #undef NB_CX
+  if (kCount) {
+    const uint32_t together = __activemask();
+    uint32_t n_tris = 0;
+    for (uint32_t lm = leaf_mask; lm; lm &= lm - 1) {
+      const int k = __ffs(lm) - 1;
+      n_tris += (((k < 4 ? m0 : m1) >> (8 * (k & 3))) & 0xFFu) >> 5;
+    }
+    const uint32_t with_leaves = __ballot_sync(together, leaf_mask != 0u);
+    const uint32_t most = __reduce_max_sync(together, n_tris);
+    if (with_leaves && lowest_active(together)) {
+      ++cnt->leaf_steps;
+      cnt->leaf_lanes += (uint32_t)__popc(with_leaves);
+      cnt->leaf_trips += most;
+    }
+  }
   // ---- BLAS leaves: Moller-Trumbore (raytracing_sw.wgsl:51-78, 274-286) ----
   while (leaf_mask) {
     const int k = __ffs(leaf_mask) - 1;
@@ -624,7 +654,7 @@ __global__ void __launch_bounds__(256) k_raygen(PathBatch pb, const WaveTables w
 // lines, agreeing branches).  The world ray stays in registers, its box-test reciprocal in
 // shared memory (WorldMixed).
 // kCount: the instrumented variant, which also adds the TraceCount totals of the launch to
-// counters[8 * bounce + 0..4] (run only when a caller asks for the counters).
+// counters[kTraceCounterSlots * bounce + ...] (run only when a caller asks for the counters).
 //
 // kRefill (bounces >= 1): a lane whose ray finished does not wait for the rest of its warp's
 // 32 rays; once kRefillIdle lanes of the warp are idle, the warp takes that many new rays with
@@ -701,15 +731,17 @@ __global__ void __launch_bounds__(kTraceThreads, kRefill ? 8 : 7) k_trace_wave(P
         &cnt, world[threadIdx.x >> 5]);
   }
   if (st) atomicOr(pb.status, st);
-  if (kCount) {
-    const uint32_t c[5] = {cnt.tlas_nodes, cnt.blas_nodes, cnt.tris, cnt.insts, cnt.pushes};
+  if (kCount) {  // counters[kTraceCounterSlots * bounce + 0..10]: see nb_pathtracer_trace_counters
+    const uint32_t c[10] = {cnt.tlas_nodes, cnt.blas_nodes, cnt.tris, cnt.insts, cnt.pushes,
+                            cnt.warp_steps, cnt.lane_steps, cnt.leaf_steps, cnt.leaf_lanes, cnt.leaf_trips};
+    unsigned long long* slot = counters + nb::kTraceCounterSlots * bounce;
 #pragma unroll
-    for (int k = 0; k < 5; ++k) {
+    for (int k = 0; k < 10; ++k) {
       unsigned long long v = c[k];
       for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xFFFFFFFFu, v, o);
-      if (lane == 0 && v) atomicAdd(counters + 8 * bounce + k, v);
+      if (lane == 0 && v) atomicAdd(slot + (k < 5 ? k : k + 1), v);
     }
-    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(counters + 8 * bounce + 5, (unsigned long long)n);
+    if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(slot + 5, (unsigned long long)n);
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) atomicAdd(ray_total, (unsigned long long)n);
 }

@@ -44,6 +44,9 @@ struct Segment {
 // to it (environment NEE, radiance cache); with the reference estimator every path's radiance
 // is written once, where the path ends (k_shade), and raygen leaves it alone.
 constexpr uint32_t kWaveZeroRadiance = 1u << 0;
+// 64-bit counters per bounce slot of the instrumented traversal (nb_pathtracer_trace_counters):
+// 0-4 node / triangle / instance / push counts, 5 rays, 6-10 warp-step statistics
+constexpr uint32_t kTraceCounterSlots = 16;
 struct WaveTables {
   uint32_t n_segs, n_jobs, n_scenes, n_paths, n_pix;
   uint32_t flags;

@@ -138,7 +138,8 @@ def test_soup_1m_any_hit_matches_oracle(soup_1m, kind):
 
 def test_trace_counters_leave_the_image_unchanged(spheres_c0):
     """The instrumented traversal (nb_pathtracer_enable_trace_counters) renders the same image
-    and counts at least one node test and one ray per traced bounce."""
+    and counts at least one node test and one ray per traced bounce; its warp-step statistics
+    are consistent with the per-lane counts."""
     desc, scene, env, cam = spheres_c0
     pt = nb.Pathtracer(256, 256, nb.Globals(bounces=6))
     pt.render(scene, cam, env, 4)
@@ -154,6 +155,15 @@ def test_trace_counters_leave_the_image_unchanged(spheres_c0):
     assert c[0]["rays"] == 256 * 256 * 4
     assert all(x["tlas_node_tests"] >= x["rays"] for x in c if x["rays"])
     assert c[0]["triangle_tests"] > 0 and c[0]["instance_entries"] > 0
+    for x in c:
+        if not x["rays"]:
+            continue
+        # warp-step statistics: every warp step has 1..32 lanes, every node test is a lane of one
+        assert 0 < x["warp_steps"] <= x["lane_steps"] <= 32 * x["warp_steps"]
+        assert x["lane_steps"] == x["tlas_node_tests"] + x["blas_node_tests"]
+        assert x["leaf_steps"] <= x["warp_steps"] and x["leaf_steps"] <= x["leaf_lanes"] <= 32 * x["leaf_steps"]
+        # the warp's leaf iterations cover every lane's triangles: at most 32 tests per iteration
+        assert x["leaf_warp_triangles"] <= x["triangle_tests"] <= 32 * x["leaf_warp_triangles"]
     pt.enable_trace_counters(False)
     with pytest.raises(nb.NbError):
         pt.trace_counters(7)
