@@ -483,11 +483,11 @@ __device__ __forceinline__ uint32_t trace_refill(uint32_t* fetch, uint32_t n, Lo
 // traversal-only query (nb_trace_rays)
 // ------------------------------------------------------------------------------------------
 // kRefill: lanes refill as they finish (trace_refill), for rays whose neighbours in the array
-// are unrelated; else each warp traces 32 consecutive rays to the end.  The refill and any-hit
-// instantiations fit 64 registers without spills and run 8 blocks per SM, closest hit without
-// refill 7 blocks at 72 registers.
+// are unrelated; else each warp traces 32 consecutive rays to the end.  Blocks per SM: 9 with
+// refill (56 registers; 1M-triangle soup, incoherent rays: 28.0 -> 26.8 ms against 8 blocks),
+// 8 for any hit without refill (64 registers), 7 for closest hit without refill (72).
 template <bool kAny, bool kRefill>
-__global__ void __launch_bounds__(kTraceThreads, kRefill || kAny ? 8 : 7)
+__global__ void __launch_bounds__(kTraceThreads, kRefill ? 9 : kAny ? 8 : 7)
     k_trace_rays(DevScene s, const float4* __restrict__ rays, uint32_t n, float4* __restrict__ hits,
                  uint32_t* __restrict__ inst, uint32_t* __restrict__ fetch, uint32_t* __restrict__ status) {
   const int lane = threadIdx.x & 31;
@@ -663,12 +663,12 @@ __global__ void __launch_bounds__(256) k_raygen(PathBatch pb, const WaveTables w
 // differ widely, so without refill most lanes idle while the longest ray finishes (11 of 32
 // lanes active per instruction on bounce 1).  Camera rays keep whole-warp chunks: a warp's 32
 // samples of one pixel finish together, and refilling them measured 9% slower traversal.
-// Refill changes only which lane traces a ray, not its result.  The refill instantiation fits
-// 64 registers without spills, so it runs 8 blocks of 128 per SM instead of 7 at 72 (measured:
-// secondary-ray traversal 2.6 ms faster per frame; 6 blocks at 80 registers 5.2 ms slower, 9
-// blocks at 56 spills).
+// Refill changes only which lane traces a ray, not its result.  The refill instantiation runs
+// 9 blocks of 128 per SM at 56 registers (8 bytes spilled); per benchmark frame 8 blocks at 64
+// registers took 1.2 ms longer and 10 at 48 (100 bytes spilled) 4.7 ms longer: secondary rays
+// wait on dependent loads, and more warps hide them.
 template <bool kSingle, bool kCount, bool kRefill>
-__global__ void __launch_bounds__(kTraceThreads, kRefill ? 8 : 7) k_trace_wave(PathBatch pb, const WaveTables wt,
+__global__ void __launch_bounds__(kTraceThreads, kRefill ? 9 : 7) k_trace_wave(PathBatch pb, const WaveTables wt,
                                                                      uint32_t bounce,
                                                        unsigned long long* __restrict__ ray_total,
                                                        unsigned long long* __restrict__ counters) {
