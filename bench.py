@@ -50,11 +50,11 @@ if ROOT not in sys.path:
 METRIC = "Mrays/s (primary + extension rays), 1920x1080 64spp 8 bounces"
 # DRAM bytes (read + write) per traversal query of k_trace_wave over all bounces of a frame,
 # from one ncu capture of the same scene at 480x270, 64 spp (nine launches, 12,435,256 rays,
-# 982.7 MB read + 480.3 MB written); the roofline scales it to a launch by the launch's rays
-TRACE_DRAM_BYTES_PER_RAY = 117.7
+# 1,015.3 MB read + 486.2 MB written); the roofline scales it to a launch by the launch's rays
+TRACE_DRAM_BYTES_PER_RAY = 120.7
 # issue utilisation of the same capture (smsp__issue_active.avg.pct_of_peak_sustained_active):
 # camera rays (k_trace_wave<1,0,0>) and bounce 1 (the lane-refill kernel)
-TRACE_ISSUE_ACTIVE_PCT = {"camera_rays": 77.4, "bounce_1": 71.8}
+TRACE_ISSUE_ACTIVE_PCT = {"camera_rays": 77.4, "bounce_1": 75.3}
 UNIT = "Mrays/s"
 WORKLOAD = "instanced 16 meshes / 1024 instances, 1920x1080, 64 spp, 8 bounces, equirect sky"
 # bytes the device layout fetches per unit of traversal work (nb_trace_counters): an 8-wide
@@ -676,7 +676,7 @@ def trace_roofline(pt, scene, cam, env, desc, kt, steps, rays_per_step, sh, of):
             "issue_active_pct": TRACE_ISSUE_ACTIVE_PCT,
             "note": "achieved = bytes the 8-wide device layout fetches (instrumented counters of one extra "
                     "frame) / timed trace launch time, against the HBM copy peak; mostly L1/L2 hits.  The "
-                    "binding limit is instruction issue (issue_active_pct: the schedulers issue in 72-77% of "
+                    "binding limit is instruction issue (issue_active_pct: the schedulers issue in 75-77% of "
                     "cycles, ncu on the 480x270 64-spp case) with SIMT divergence, not DRAM bandwidth"}
     if of is not None:
         n_aabb, n_tri, n_inst = of.work_per_ray()
