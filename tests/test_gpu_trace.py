@@ -138,6 +138,35 @@ def test_axis_aligned_and_surface_origin_rays_match_oracle(soup):
     assert np.all(hits[:, 0][hits[:, 0] != NO_HIT] >= 0.1)
 
 
+def test_small_large_and_power_of_two_direction_components_match_oracle(soup):
+    """The box test takes its reciprocal directions from the hardware's approximate reciprocal
+    and covers that rounding by per-axis plane margins; the triangle test divides exactly.
+    Directions (not normalised: the query takes any direction) whose components sit around the
+    1e-20 nudge, far below the others, at exact powers of two, or spread over 16 decades find
+    the oracle's closest hits."""
+    desc, gpu, orc = soup
+    rng = np.random.default_rng(33)
+    n = 8000
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, :3] = rng.uniform(-1.2, 1.2, (n, 3))
+    d = rng.normal(size=(n, 3))
+    rows = np.arange(n)
+    small = np.array([1e-21, 9.9e-21, 1e-20, 1.01e-20, 1e-19, 2.0 ** -60, 1e-12, 1e-6])
+    which = rng.integers(0, 3, n)
+    d[rows, which] = np.where(d[rows, which] < 0, -1.0, 1.0) * small[rng.integers(0, len(small), n)]
+    q = n // 4  # exact powers of two, whose reciprocals are exact
+    d[:q] = np.where(d[:q] < 0, -1.0, 1.0) * 2.0 ** rng.integers(-10, 11, (q, 3))
+    e = n // 8  # components spread over 16 decades
+    d[q:q + e] *= 10.0 ** rng.integers(-8, 9, (e, 3))
+    rays[:, 4:7] = d
+    assert np.all(np.isfinite(rays))
+    hits, inst = gpu.trace_host(rays)
+    rf, ru, cnt = orc.trace(rays)
+    assert cnt[:, 3].max() == 0
+    ties, both = compare_hits(hits, inst, gpu.export()["indices"], rf, ru)
+    assert both > 300  # 480 of the 8000 rays hit the sparse soup
+
+
 def test_non_finite_rays_hit_nothing(soup):
     """Rays with a NaN or infinite origin or direction component meet nothing, as in the
     oracle (every slab and triangle comparison of the reference fails on NaN); finite rays
